@@ -1,0 +1,218 @@
+/*
+ * tagpu — C ABI of the GB300-native block-sparse contraction engine.
+ *
+ * The engine replaces TiledArray's block-sparse contraction path
+ *   C("i,j") = A("i,k") * B("k,j"),  R("a,b,i,j") = V("a,b,c,d") * T("c,d,i,j")
+ * on one GPU.  Every entry point is extern "C", takes plain pointers and
+ * sizes, and returns a tagpu_status; nothing throws across this boundary.
+ * The message of the last failure on a context is tagpu_last_error().
+ *
+ * Reference interfaces replaced (paths relative to the TiledArray source):
+ *   tagpu_init / tagpu_shutdown       TiledArray::initialize / finalize
+ *                                     (tiledarray.cpp:84-185)
+ *   tagpu_threshold_get / _set        SparseShape<float>::threshold()
+ *                                     (sparse_shape.h:548-557, 1941-1942)
+ *   tagpu_array_create                DistArray(world, TiledRange[, shape])
+ *                                     (dist_array.h:63; tiled_range.h:33;
+ *                                      tiled_range1.h:47)
+ *   tagpu_array_set_shape             SparseShape(norms, trange[, do_not_scale])
+ *                                     (sparse_shape.h:335-348, 407-422)
+ *   tagpu_array_upload / _download    DistArray::set / find of Tensor tiles
+ *   tagpu_array_generate              make_array with a per-tile norm op
+ *                                     (conversions/make_array.h:151-199) over
+ *                                     device-generated tiles
+ *   tagpu_contract                    TsrExpr::operator= of a contraction
+ *                                     (expressions/tsr_expr.h:132-138 ->
+ *                                      expr.h:377-430 -> cont_engine.h:354-677
+ *                                      -> dist_eval/contraction_eval.h)
+ *   tagpu_shape_gemm                  SparseShape::gemm (sparse_shape.h:1589-1684)
+ *   tagpu_pair_list                   Summa tile-pair set
+ *                                     (dist_eval/contraction_eval.h:630-650,
+ *                                      1093-1161, 1348-1384)
+ *   tagpu_permute                     Tensor permute (tensor/permute.h:124-210)
+ *   tagpu_batch_*                     many independent TsrExpr assignments
+ *                                     evaluated together (one persistent launch)
+ *   tagpu_server_*                    no counterpart: request loop for served
+ *                                     contractions
+ *
+ * Ownership: arrays are owned by the caller and freed with
+ * tagpu_array_destroy; device storage belongs to the context.  Host buffers
+ * passed in are copied before the call returns.
+ * Threading: a context serialises its own work; tagpu_server_submit may be
+ * called from many host threads.
+ */
+#ifndef TAGPU_H
+#define TAGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tagpu_status {
+  TAGPU_OK = 0,
+  TAGPU_ERR_INVALID = 1,      /* malformed argument (TA_EXCEPTION analogue) */
+  TAGPU_ERR_UNSUPPORTED = 2,  /* expression form not on this path */
+  TAGPU_ERR_NOMEM = 3,        /* device allocation failed or over budget */
+  TAGPU_ERR_CUDA = 4,         /* CUDA runtime error */
+  TAGPU_ERR_TIMEOUT = 5,      /* a bounded device or host wait ran out */
+  TAGPU_ERR_REJECTED = 6,     /* server admission rejected the request */
+  TAGPU_ERR_NOT_READY = 7,    /* server request still in flight */
+  TAGPU_ERR_STATE = 8         /* object used in the wrong state */
+} tagpu_status;
+
+typedef enum tagpu_precision {
+  TAGPU_PRECISION_FP64 = 0,   /* plain FP64: DMMA (mma.sync f64) */
+  TAGPU_PRECISION_OZAKI = 1   /* emulated FP64: exact integer slices on the
+                                 tcgen05 tensor cores, FP64 recombination */
+} tagpu_precision;
+
+typedef struct tagpu_config {
+  int device;                 /* CUDA device ordinal */
+  size_t hbm_budget_bytes;    /* 0 = no budget */
+} tagpu_config;
+
+typedef struct tagpu_ctx tagpu_ctx;
+typedef struct tagpu_array tagpu_array;
+
+tagpu_status tagpu_init(const tagpu_config* cfg, tagpu_ctx** out);
+tagpu_status tagpu_shutdown(tagpu_ctx* ctx);
+const char* tagpu_last_error(const tagpu_ctx* ctx);
+const char* tagpu_status_string(tagpu_status s);
+/* Blocks until all work queued on the context has finished. */
+tagpu_status tagpu_sync(tagpu_ctx* ctx);
+
+/* Default screening threshold used for new result shapes; initial value is
+ * FLT_EPSILON as in SparseShape<float>. */
+float tagpu_threshold_get(const tagpu_ctx* ctx);
+void tagpu_threshold_set(tagpu_ctx* ctx, float threshold);
+
+/* ---- arrays --------------------------------------------------------------
+ * hashmarks[d] holds ntiles[d]+1 increasing boundaries of dimension d
+ * (TiledRange1).  rank <= 8.  A new array is dense (DensePolicy) until a
+ * shape is set. */
+tagpu_status tagpu_array_create(tagpu_ctx* ctx, int rank, const int64_t* ntiles,
+                                const int64_t* const* hashmarks,
+                                tagpu_array** out);
+tagpu_status tagpu_array_destroy(tagpu_array* a);
+
+/* SparseShape semantics: norms holds one Frobenius norm per tile (tile grid,
+ * row-major).  Unless do_not_scale, they are divided by the tile volume;
+ * values below `threshold` (negative: the context default) are zeroed.
+ * Passing norms == NULL makes the array dense. */
+tagpu_status tagpu_array_set_shape(tagpu_array* a, const float* norms,
+                                   int do_not_scale, float threshold);
+
+/* Host tiles: the nonzero tiles in tile-ordinal order, each row-major over
+ * its own range, concatenated; n = total element count
+ * (tagpu_array_info().elements). */
+tagpu_status tagpu_array_upload(tagpu_array* a, const double* tiles, int64_t n);
+tagpu_status tagpu_array_download(const tagpu_array* a, double* tiles, int64_t n);
+
+/* Device-side synthetic operand: element with global ordinal g in tile t
+ * gets value(seed, stream, g) * tile_scale[t]; kind 0 = uniform[-1,1),
+ * kind 1 = integers hash % 101.  Tiles with tile_scale[t] == 0 are absent.
+ * tile_scale == NULL means 1 for every tile.  If compute_shape, the shape is
+ * set from the device tile norms (make_array semantics) with `threshold`
+ * (negative: context default) and tiles below it are dropped. */
+tagpu_status tagpu_array_generate(tagpu_array* a, uint64_t seed, uint64_t stream,
+                                  int kind, const double* tile_scale,
+                                  int compute_shape, float threshold);
+
+typedef struct tagpu_array_info {
+  int rank;
+  int dense;                  /* 1: DensePolicy */
+  int64_t ntiles_total;       /* tile-grid volume */
+  int64_t nonzero_tiles;
+  int64_t zero_tiles;         /* SparseShape zero_tile_count */
+  int64_t elements;           /* stored elements (sum of nonzero tile volumes) */
+  float threshold;            /* the shape's own threshold */
+  size_t device_bytes;
+  int64_t ntiles[8];          /* tiles per dimension (first `rank` entries) */
+} tagpu_array_info;
+tagpu_status tagpu_array_get_info(const tagpu_array* a, tagpu_array_info* info);
+/* Scaled tile norms (tile grid, row-major). */
+tagpu_status tagpu_array_get_norms(const tagpu_array* a, float* norms);
+/* Element offset of every tile in the upload/download buffer, -1 if zero. */
+tagpu_status tagpu_array_get_tile_offsets(const tagpu_array* a, int64_t* offsets);
+/* Tiling of the array: hashmarks of dimension d (ntiles[d]+1 values). */
+tagpu_status tagpu_array_get_hashmarks(const tagpu_array* a, int d,
+                                       int64_t* hashmarks);
+
+/* ---- contraction -------------------------------------------------------- */
+typedef struct tagpu_contract_opts {
+  int precision;              /* tagpu_precision */
+  int slices;                 /* Ozaki slices per operand, 0 = default (6) */
+  float threshold;            /* result screening threshold, <0 = default */
+} tagpu_contract_opts;
+
+typedef struct tagpu_contract_stats {
+  int64_t result_tiles;       /* M_t * N_t */
+  int64_t nonzero_result_tiles;
+  int64_t zero_tiles;         /* result SparseShape zero count */
+  int64_t pairs;              /* |tile-pair list| */
+  double flops;               /* 2 * sum over pairs of m*k*n */
+  double ms_shape;            /* kernel (a) */
+  double ms_pairs;            /* kernel (b) */
+  double ms_permute;          /* kernel (c), arguments and result */
+  double ms_split;            /* Ozaki slicing */
+  double ms_gemm;             /* kernel (d) */
+  double ms_total;            /* whole call, host wall clock */
+  int left_permtype, right_permtype; /* 1 identity, 2 transpose, 3 general */
+  int precision;
+  int slices;
+  int64_t gemm_blocks;        /* output blocks the GEMM ran */
+  int64_t gemm_launches;      /* kernels launched by the call */
+} tagpu_contract_stats;
+
+/* c = alpha * A(a_idx) * B(b_idx) with index strings like "i,k".  *c is a new
+ * array (the target); the result shape is SparseShape::gemm of the argument
+ * shapes with the result threshold. */
+tagpu_status tagpu_contract(tagpu_ctx* ctx, const char* c_idx, double alpha,
+                            tagpu_array* A, const char* a_idx, tagpu_array* B,
+                            const char* b_idx, const tagpu_contract_opts* opts,
+                            tagpu_array** c);
+tagpu_status tagpu_last_stats(const tagpu_ctx* ctx, tagpu_contract_stats* st);
+
+/* ---- single steps, host buffers (for parity tests) ----------------------- */
+/* Kernel (a): result[M x N] = |factor| * (left[M x K] * k_sizes) x
+ * (right[K x N] * k_sizes) in float, k ascending, screened by threshold.
+ * K == 0 (k_sizes NULL) is the outer-product branch. */
+tagpu_status tagpu_shape_gemm(tagpu_ctx* ctx, int64_t M, int64_t N, int64_t K,
+                              const float* left, const float* right,
+                              const float* k_sizes, double factor,
+                              float threshold, float* result,
+                              int64_t* zero_count);
+/* Kernel (b): CSR tile-pair list.  offsets: M*N+1; kidx capacity kidx_cap
+ * (pass kidx NULL to count only). */
+tagpu_status tagpu_pair_list(tagpu_ctx* ctx, int64_t M, int64_t N, int64_t K,
+                             const float* cnorm, float c_thr,
+                             const float* lnorm, float l_thr,
+                             const float* rnorm, float r_thr, int64_t* offsets,
+                             int32_t* kidx, int64_t kidx_cap, int64_t* npairs);
+/* Kernel (c): out = permute(in, perm), result dim perm[d] = arg dim d. */
+tagpu_status tagpu_permute(tagpu_ctx* ctx, int rank, const int64_t* extents,
+                           const int32_t* perm, const double* in, double* out);
+
+/* ---- batched evaluation --------------------------------------------------- */
+typedef struct tagpu_batch tagpu_batch;
+tagpu_status tagpu_batch_create(tagpu_ctx* ctx, tagpu_batch** out);
+/* Adds c = alpha * A(a_idx) * B(b_idx); *c is created now and filled by run. */
+tagpu_status tagpu_batch_add(tagpu_batch* b, const char* c_idx, double alpha,
+                             tagpu_array* A, const char* a_idx, tagpu_array* B,
+                             const char* b_idx, const tagpu_contract_opts* opts,
+                             tagpu_array** c);
+/* First call plans every contraction and captures the launch sequence in a
+ * CUDA graph; later calls replay the graph (operands may change values, not
+ * shapes). */
+tagpu_status tagpu_batch_run(tagpu_batch* b);
+tagpu_status tagpu_batch_stats(const tagpu_batch* b, tagpu_contract_stats* st);
+tagpu_status tagpu_batch_destroy(tagpu_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TAGPU_H */

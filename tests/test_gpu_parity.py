@@ -1,0 +1,214 @@
+"""GPU parity: every kernel on the path against the CPU oracle, through the C ABI.
+
+Bit-exact for the screened shapes, pair lists, permutations and integer-valued
+contractions; relative Frobenius error <= 1e-12 for uniform[-1,1) data.
+"""
+import numpy as np
+import pytest
+
+from helpers import contraction_cases, golden, gpu_operand, oracle_operand, rel_fro
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12  # relative Frobenius error bound for floating-point data
+
+
+@pytest.fixture(scope="module")
+def ta():
+    import tiledarray_gb300 as ta
+    return ta
+
+
+def uneven_hashmarks(n_total, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    h = [0]
+    while h[-1] < n_total:
+        h.append(min(n_total, h[-1] + int(rng.integers(lo, hi + 1))))
+    return h
+
+
+@pytest.mark.parametrize("tr_dims,kind", [
+    ([[0, 2, 5, 10, 17, 28]] * 3, 1),
+    ([[0, 13, 40, 64], [0, 7, 31, 50]], 0),
+    ([uneven_hashmarks(700, 32, 256, 1), uneven_hashmarks(500, 32, 256, 2)], 0),
+    ([[0, 3, 7, 8], [0, 2, 6], [0, 3, 7, 8], [0, 2, 6]], 0),
+])
+def test_generate_and_shape_bitexact(oracle, ta, world, tr_dims, kind):
+    n = int(np.prod([len(h) - 1 for h in tr_dims]))
+    keep = (np.arange(n) % 3) != 1
+    Ao = oracle_operand(oracle, tr_dims, 9, 4, kind=kind, keep=keep)
+    Ag, tr = gpu_operand(ta, world, tr_dims, 9, 4, kind=kind, keep=keep)
+    assert np.array_equal(Ag.norms(), Ao.norms.ravel())
+    got = Ag.tiles(tr)
+    assert set(got) == set(Ao.tiles)
+    for o, t in Ao.tiles.items():
+        assert np.array_equal(got[o], t)
+
+
+def test_shape_gemm_kernel_matches_golden(oracle, ta, world):
+    g = golden("shape_gemm.npz")
+    tr = [list(h) for h in g["hashmarks"]]
+    sizes = [np.asarray([h[i + 1] - h[i] for i in range(len(h) - 1)], np.float32) for h in tr]
+    ks = oracle.outer_sizes([5, 5], np.concatenate(sizes[1:]), False)
+    L, R = g["left"].reshape(5, 25), g["right"].reshape(25, 5)
+    r_o, z_o = oracle.shape_gemm(L, R, ks, float(g["factor"]), float(g["threshold"]))
+    r_g, z_g = world.shape_gemm(L, R, ks, float(g["factor"]), float(g["threshold"]))
+    assert np.array_equal(r_g, r_o) and z_g == z_o
+
+
+@pytest.mark.parametrize("M,N,K,seed", [(1, 1, 1, 0), (106, 106, 106, 1), (36, 9, 36, 2),
+                                        (300, 7, 1000, 3), (5, 333, 0, 4)])
+def test_shape_gemm_kernel_bitexact(oracle, ta, world, M, N, K, seed):
+    rng = np.random.default_rng(seed)
+    L = (rng.random((M, max(K, 1))) ** 4).astype(np.float32) * 1e-3
+    R = (rng.random((max(K, 1), N)) ** 4).astype(np.float32) * 1e-3
+    L[rng.random(L.shape) < 0.3] = 0
+    ks = rng.integers(16, 9216, K).astype(np.float32) if K else None
+    thr = np.float32(1e-8)
+    r_o, z_o = oracle.shape_gemm(L, R, ks, -2.5, thr)
+    r_g, z_g = world.shape_gemm(L, R, ks, -2.5, thr)
+    assert np.array_equal(r_g, r_o) and z_g == z_o
+
+
+def test_pair_list_kernel_matches_golden(ta, world):
+    g = golden("pairs.npz")
+    for c in range(int(g["ncases"])):
+        thr = g[f"c{c}_thr"]
+        offs, kidx = world.pair_list(g[f"c{c}_C"], thr[0], g[f"c{c}_L"], thr[1], g[f"c{c}_R"],
+                                     thr[2])
+        assert np.array_equal(offs, g[f"c{c}_offsets"])
+        assert np.array_equal(kidx, g[f"c{c}_kidx"])
+
+
+def test_pair_list_kernel_large(oracle, ta, world):
+    rng = np.random.default_rng(7)
+    M, N, K = 120, 110, 130
+    C, L, R = (rng.random((M, N), np.float32), rng.random((M, K), np.float32),
+               rng.random((K, N), np.float32))
+    o1, k1 = oracle.pairs(C, 0.3, L, 0.5, R, 0.2)
+    o2, k2 = world.pair_list(C, 0.3, L, 0.5, R, 0.2)
+    assert np.array_equal(o1, o2) and np.array_equal(k1, k2)
+
+
+def test_permute_kernel_matches_golden(ta, world):
+    g = golden("permute.npz")
+    for c in range(int(g["ncases"])):
+        y = world.permute(g[f"c{c}_x"], list(g[f"c{c}_perm"]))
+        assert np.array_equal(y, g[f"c{c}_y"])
+
+
+@pytest.mark.parametrize("shape,perm", [((96, 80, 64, 32), (3, 1, 2, 0)),
+                                        ((256, 255), (1, 0)), ((33, 17, 65), (0, 2, 1)),
+                                        ((9, 96, 96), (1, 2, 0))])
+def test_permute_kernel_large(oracle, ta, world, shape, perm):
+    x = np.random.default_rng(1).random(shape)
+    assert np.array_equal(world.permute(x, perm), oracle.permute(x, perm))
+
+
+@pytest.mark.parametrize("case", contraction_cases(), ids=lambda c: c["tag"])
+def test_contraction_dmma_golden(oracle, ta, world, case):
+    """Reference test forms on integer data: exact equality with the golden
+    dense result, result shape bit-exact with the oracle."""
+    A, tra = gpu_operand(ta, world, case["trange_a"], *case["seed_a"], kind=1,
+                         keep=case["keep_a"])
+    B, trb = gpu_operand(ta, world, case["trange_b"], *case["seed_b"], kind=1,
+                         keep=case["keep_b"])
+    C, st = ta.contract(world, case["c"], case["alpha"], A, case["a"], B, case["b"])
+    exp = golden(f"contract_{case['tag']}.npz")["expected"]
+    got = C.to_dense(C.trange)
+    assert np.array_equal(got, exp)
+    Ao = oracle_operand(oracle, case["trange_a"], *case["seed_a"], kind=1, keep=case["keep_a"])
+    Bo = oracle_operand(oracle, case["trange_b"], *case["seed_b"], kind=1, keep=case["keep_b"])
+    Co, info = oracle.contract(case["c"], Ao, case["a"], Bo, case["b"], case["alpha"],
+                               return_pairs=True)
+    assert np.array_equal(C.norms(), Co.norms.ravel())
+    assert st["pairs"] == len(info["kidx"])
+    assert st["left_permtype"] == info["left_permtype"]
+    assert st["right_permtype"] == info["right_permtype"]
+
+
+def block_sparse_case(n, lo, hi, seed, decay=4.0, cut=1e-10):
+    h = uneven_hashmarks(n, lo, hi, seed)
+    nt = len(h) - 1
+    I, J = np.meshgrid(np.arange(nt), np.arange(nt), indexing="ij")
+    scale = np.exp(-np.abs(I - J) / decay)
+    scale[scale < cut] = 0.0
+    return h, scale
+
+
+@pytest.mark.parametrize("n,lo,hi,seed", [(600, 48, 256, 1), (1000, 32, 128, 2),
+                                          (257, 1, 64, 3)])
+def test_contraction_dmma_uniform(oracle, ta, world, n, lo, hi, seed):
+    h, scale = block_sparse_case(n, lo, hi, seed, decay=2.0)
+    thr = 1e-8
+    A, tr = gpu_operand(ta, world, [h, h], seed, 0, kind=0, tile_scale=scale, threshold=thr)
+    B, _ = gpu_operand(ta, world, [h, h], seed, 1, kind=0, tile_scale=scale, threshold=thr)
+    world.threshold = thr
+    try:
+        C, st = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j")
+    finally:
+        world.threshold = ta.FLT_EPSILON
+    Ao = oracle_operand(oracle, [h, h], seed, 0, kind=0, tile_scale=scale, threshold=thr)
+    Bo = oracle_operand(oracle, [h, h], seed, 1, kind=0, tile_scale=scale, threshold=thr)
+    Co, info = oracle.contract("i,j", Ao, "i,k", Bo, "k,j", threshold=thr, return_pairs=True)
+    assert np.array_equal(C.norms(), Co.norms.ravel())
+    assert st["pairs"] == len(info["kidx"])
+    ref = Co.to_dense()
+    got = C.to_dense(C.trange)
+    assert rel_fro(got, ref) <= TOL
+
+
+def test_batch_graph_replay(oracle, ta, world):
+    import ctypes
+    L = world.L
+    forms = [("i,j", "i,k", "k,j"), ("i,j", "k,i", "k,j"), ("j,i", "i,k", "j,k")]
+    h1 = uneven_hashmarks(300, 20, 90, 5)
+    h2 = uneven_hashmarks(260, 20, 90, 6)
+    ops = []
+    for x, (c, a, b) in enumerate(forms):
+        tra = [h1, h2] if a == "i,k" else [h2, h1]
+        trb = [h2, h1] if b == "k,j" else [h1, h2]
+        A, _ = gpu_operand(ta, world, tra, 3, 2 * x, kind=0)
+        B, _ = gpu_operand(ta, world, trb, 3, 2 * x + 1, kind=0)
+        ops.append((c, a, b, A, B))
+    bh = ctypes.c_void_p()
+    world.check(L.tagpu_batch_create(world.h, ctypes.byref(bh)))
+    outs = []
+    for c, a, b, A, B in ops:
+        ch = ctypes.c_void_p()
+        opts = ta.ContractOpts(ta.PRECISION_FP64, 0, -1.0)
+        world.check(L.tagpu_batch_add(bh, c.encode(), 1.0, A.h, a.encode(), B.h, b.encode(),
+                                      ctypes.byref(opts), ctypes.byref(ch)))
+        outs.append(ta.DistArray(world, _handle=ch))
+    world.check(L.tagpu_batch_run(bh))
+    first = [o.download().copy() for o in outs]
+    for c, a, b, A, B in ops:
+        ref, _ = ta.contract(world, c, 1.0, A, a, B, b)
+        assert np.array_equal(ref.download(), first[ops.index((c, a, b, A, B))])
+    world.check(L.tagpu_batch_run(bh))  # graph replay
+    for o, f in zip(outs, first):
+        assert np.array_equal(o.download(), f)
+    world.check(L.tagpu_batch_destroy(bh))
+
+
+def test_invalid_and_unsupported_forms(ta, world):
+    A, _ = gpu_operand(ta, world, [[0, 4, 8], [0, 3, 6]], 1, 0, kind=0)
+    B, _ = gpu_operand(ta, world, [[0, 3, 6], [0, 5]], 1, 1, kind=0)
+    with pytest.raises(ta.TAGPUError) as e:
+        ta.contract(world, "i,j", 1.0, A, "i,j", B, "i,j")  # Hadamard
+    assert e.value.status == 2
+    with pytest.raises(ta.TAGPUError) as e:
+        ta.contract(world, "i,j", 1.0, A, "i,k", B, "j,k")  # k tilings not congruent
+    assert e.value.status == 1
+    with pytest.raises(ta.TAGPUError) as e:
+        ta.contract(world, "i,j", 1.0, A, "i,,k", B, "k,j")
+    assert e.value.status == 1
+
+
+def test_all_screened_result(ta, world):
+    h = [0, 10, 20]
+    A, _ = gpu_operand(ta, world, [h, h], 1, 0, kind=0, tile_scale=np.full(4, 1e-6))
+    B, _ = gpu_operand(ta, world, [h, h], 1, 1, kind=0, tile_scale=np.full(4, 1e-6))
+    C, st = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j")
+    assert st["nonzero_result_tiles"] == 0 and st["pairs"] == 0
+    assert C.info().elements == 0

@@ -1,0 +1,101 @@
+// Internal declarations shared by the host library (tagpu.cpp) and the
+// kernel translation units (*.cu).  Not part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/tagpu.h"
+
+namespace tagpu {
+
+// ---------------------------------------------------------------------------
+// kernel launchers (defined in the .cu files); all asynchronous on `s`
+// ---------------------------------------------------------------------------
+
+// (a) SparseShape::gemm screening: float, k ascending, no FMA.
+void launch_shape_gemm(cudaStream_t s, int64_t M, int64_t N, int64_t K,
+                       const float* L, const float* R, const float* ksz,
+                       float abs_factor, float thr, float* C,
+                       unsigned long long* zero_count);
+
+// (b) pair list: per-result-tile counts and flops, exclusive scan, emission.
+void launch_pair_count(cudaStream_t s, int64_t M, int64_t N, int64_t K,
+                       const float* C, float cthr, const float* L, float lthr,
+                       const float* R, float rthr, const int32_t* msz,
+                       const int32_t* nsz, const int32_t* ksz, int64_t* counts,
+                       double* flops);
+void launch_exclusive_scan(cudaStream_t s, const int64_t* in, int64_t n,
+                           int64_t* out /* n+1 */);
+void launch_pair_emit(cudaStream_t s, int64_t M, int64_t N, int64_t K,
+                      const float* C, float cthr, const float* L, float lthr,
+                      const float* R, float rthr, const int64_t* offsets,
+                      int32_t* kidx);
+
+// (c) tile permutation.  Tiles of one array share `perm`; each tile has its
+// own extents.  ext: ntiles x rank argument extents; in_off / out_off:
+// element offsets; item_start: ntiles+1 prefix sums of per-tile work items.
+struct PermuteDesc {
+  int rank;
+  int perm[8];
+};
+void launch_permute(cudaStream_t s, const PermuteDesc& d, int64_t ntiles,
+                    const int32_t* ext, const int64_t* in_off,
+                    const int64_t* out_off, const int64_t* item_start,
+                    int64_t nitems, const double* in, double* out);
+// Work items a tile of the given extents needs (host-side helper shared with
+// the kernel's decomposition).
+int64_t permute_items(const PermuteDesc& d, const int64_t* ext);
+
+// Generation of synthetic operands and sequential tile norms.
+struct GenDesc {
+  int rank;
+  int64_t gext[8];    // global element extents
+  uint64_t seed, stream;
+  int kind;
+};
+void launch_generate(cudaStream_t s, const GenDesc& g, int64_t ntiles,
+                     const int64_t* tile_lo /* ntiles x rank */,
+                     const int32_t* tile_ext /* ntiles x rank */,
+                     const int64_t* tile_off /* ntiles+1 prefix */,
+                     const double* tile_scale, double* data);
+void launch_tile_norms(cudaStream_t s, int64_t ntiles, const int64_t* tile_off,
+                       const double* data, float* norms);
+
+// (d) plain FP64 DMMA GEMM over the pair list.
+struct GemmView {
+  int64_t Mt, Nt, Kt;
+  const int32_t* msz;     // Mt fused row sizes
+  const int32_t* nsz;     // Nt
+  const int32_t* ksz;     // Kt
+  const double* A;        // left tile data
+  const int64_t* aoff;    // Mt*Kt offsets, -1 absent
+  int a_trans;            // tile stored k x m
+  const double* B;
+  const int64_t* boff;    // Kt*Nt
+  int b_trans;            // tile stored n x k
+  const int64_t* poff;    // Mt*Nt+1 pair offsets
+  const int32_t* kidx;    // pair k
+  double alpha;
+  double* C;
+  const int64_t* coff;    // Mt*Nt result offsets, -1 zero tile
+};
+// One 64x64 output block of one result tile of one contraction.
+struct WorkItem {
+  int64_t tile;       // result tile ordinal (row-major over Mt x Nt)
+  int32_t view;       // index into the GemmView array
+  int16_t rb, cb;     // 64-row / 64-column block within the tile
+};
+void launch_dmma_gemm(cudaStream_t s, const GemmView* views, const WorkItem* items,
+                      int64_t nitems, int sm_count);
+
+// (d) emulated FP64 (Ozaki scheme, bf16 digit slices on tcgen05).
+struct OzakiPlan;
+tagpu_status ozaki_run(cudaStream_t s, const GemmView& v, int slices,
+                       int sm_count, size_t* scratch_bytes, double* ms_split,
+                       double* ms_gemm, int64_t* blocks, std::string* err);
+
+}  // namespace tagpu

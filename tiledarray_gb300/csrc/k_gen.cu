@@ -1,0 +1,97 @@
+// Device-side synthetic operands and tile norms, for sm_103a.
+//
+// Values: element with global ordinal g (row-major over the array's element
+// range) of tile t is value(seed, stream, g) * scale[t], where value is a
+// counter-based hash (splitmix64) mapped to uniform[-1,1) or to the integers
+// 0..100 (the `rand() % 101` data of the reference's tests).  The same
+// definition is used on the host, so operands are identical everywhere.
+//
+// Norms: Tensor::norm (tensor/tensor.h:3768-3787) is sqrt of a sequential
+// double sum of x*x in storage order (math/vector_op.h:561-577), stored as
+// float.  One thread walks one tile in that order, rounding every product and
+// sum separately, so the norms (and the SparseShape built from them) match
+// the host bit for bit.
+#include <cuda_runtime.h>
+
+#include "internal.h"
+
+namespace tagpu {
+namespace {
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+__global__ void generate_kernel(GenDesc g, int64_t ntiles,
+                                const int64_t* __restrict__ tile_lo,
+                                const int32_t* __restrict__ tile_ext,
+                                const int64_t* __restrict__ tile_off,
+                                const double* __restrict__ tile_scale,
+                                double* __restrict__ data) {
+  const int64_t total = tile_off[ntiles];
+  const uint64_t key = splitmix64(g.seed * 0x9E3779B97F4A7C15ull + g.stream);
+  int64_t gstride[8];
+  int64_t s = 1;
+  for (int d = g.rank - 1; d >= 0; --d) {
+    gstride[d] = s;
+    s *= g.gext[d];
+  }
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t lo = 0, hi = ntiles;
+    while (hi - lo > 1) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (tile_off[mid] <= e) lo = mid; else hi = mid;
+    }
+    const int64_t t = lo;
+    int64_t local = e - tile_off[t];
+    int64_t gord = 0;
+    for (int d = g.rank - 1; d >= 0; --d) {
+      const int64_t ext = tile_ext[t * g.rank + d];
+      const int64_t ix = local % ext;
+      local /= ext;
+      gord += (tile_lo[t * g.rank + d] + ix) * gstride[d];
+    }
+    const uint64_t h = splitmix64(key ^ (uint64_t)gord);
+    double v = g.kind == 1 ? (double)(h % 101ull)
+                           : __dsub_rn(__dmul_rn(__dmul_rn((double)(h >> 11), 0x1.0p-53), 2.0), 1.0);
+    data[e] = __dmul_rn(v, tile_scale ? tile_scale[t] : 1.0);
+  }
+}
+
+__global__ void tile_norms_kernel(int64_t ntiles, const int64_t* __restrict__ tile_off,
+                                  const double* __restrict__ data, float* __restrict__ norms) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  const double* x = data + tile_off[t];
+  const int64_t n = tile_off[t + 1] - tile_off[t];
+  double s = 0.0;
+  for (int64_t i = 0; i < n; ++i) s = __dadd_rn(s, __dmul_rn(x[i], x[i]));
+  norms[t] = __double2float_rn(__dsqrt_rn(s));
+}
+
+}  // namespace
+
+void launch_generate(cudaStream_t s, const GenDesc& g, int64_t ntiles,
+                     const int64_t* tile_lo, const int32_t* tile_ext,
+                     const int64_t* tile_off, const double* tile_scale, double* data) {
+  if (ntiles <= 0) return;
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  generate_kernel<<<sms * 8, 256, 0, s>>>(g, ntiles, tile_lo, tile_ext, tile_off, tile_scale,
+                                          data);
+}
+
+void launch_tile_norms(cudaStream_t s, int64_t ntiles, const int64_t* tile_off,
+                       const double* data, float* norms) {
+  if (ntiles <= 0) return;
+  const int threads = 64;
+  tile_norms_kernel<<<(unsigned)((ntiles + threads - 1) / threads), threads, 0, s>>>(
+      ntiles, tile_off, data, norms);
+}
+
+}  // namespace tagpu

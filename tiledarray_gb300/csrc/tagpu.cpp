@@ -1,0 +1,1577 @@
+// tagpu host library: the C ABI of include/tagpu.h.
+//
+// The expression semantics are TiledArray's (paths relative to its source):
+//   index parsing / product classification  expressions/mult_engine.h:300-360
+//   layout choice (permtypes)               expressions/permopt.h:258-396,
+//                                           expressions/binary_engine.h:101-176
+//   fused GEMM dimensions                   math/gemm_helper.h:57-90, 252-273
+//   result tiling and shape                 expressions/cont_engine.h:354-535,
+//                                           642-677
+//   shape construction and scaling          sparse_shape.h:150-237, 335-422
+// Host code only plans; every step that touches tile data or norms runs in a
+// kernel (k_*.cu).  Compiled with -ffp-contract=off: the float shape algebra
+// done here (size vectors, scaling) rounds each operation separately, as the
+// CPU reference does.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+using namespace tagpu;
+
+// ---------------------------------------------------------------------------
+// context and arrays
+// ---------------------------------------------------------------------------
+
+struct tagpu_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  float threshold = std::numeric_limits<float>::epsilon();
+  size_t budget = 0;
+  std::atomic<size_t> used{0};
+  std::string err;
+  tagpu_contract_stats last{};
+  std::recursive_mutex mu;
+};
+
+struct tagpu_array {
+  tagpu_ctx* ctx = nullptr;
+  int rank = 0;
+  std::vector<std::vector<int64_t>> hm;  // hashmarks per dim
+  std::vector<int64_t> nt;               // tiles per dim
+  bool dense = true;
+  std::vector<float> norms;              // scaled norms (sparse only)
+  float threshold = 0.0f;                // the shape's own threshold
+  int64_t zero_count = 0;
+  std::vector<int64_t> off;              // element offset per tile, -1 zero
+  int64_t elements = 0;
+  double* data = nullptr;                // device
+  size_t bytes = 0;
+
+  int64_t ntiles() const {
+    int64_t n = 1;
+    for (auto x : nt) n *= x;
+    return n;
+  }
+  void tile_index(int64_t ord, int64_t* idx) const {
+    for (int d = rank - 1; d >= 0; --d) {
+      idx[d] = nt[d] ? ord % nt[d] : 0;
+      ord = nt[d] ? ord / nt[d] : 0;
+    }
+  }
+  int64_t tile_volume(int64_t ord) const {
+    int64_t idx[8];
+    tile_index(ord, idx);
+    int64_t v = 1;
+    for (int d = 0; d < rank; ++d) v *= hm[d][idx[d] + 1] - hm[d][idx[d]];
+    return v;
+  }
+  bool tile_is_zero(int64_t ord) const {
+    if (dense) return false;
+    return norms[ord] < threshold;
+  }
+  ~tagpu_array();  // releases the device storage
+};
+
+namespace {
+
+tagpu_status fail(tagpu_ctx* ctx, tagpu_status st, const char* fmt, ...) {
+  if (ctx) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    ctx->err = buf;
+  }
+  return st;
+}
+
+#define CUDA_TRY(ctx, call)                                                          \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess)                                                           \
+      return fail((ctx), TAGPU_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+tagpu_status dev_alloc(tagpu_ctx* ctx, void** p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) return TAGPU_OK;
+  if (ctx->budget && ctx->used.load() + bytes > ctx->budget)
+    return fail(ctx, TAGPU_ERR_NOMEM, "device budget exceeded: %zu + %zu > %zu bytes",
+                ctx->used.load(), bytes, ctx->budget);
+  cudaError_t e = cudaMallocAsync(p, bytes, ctx->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, TAGPU_ERR_NOMEM, "cudaMallocAsync(%zu) failed: %s", bytes,
+                cudaGetErrorString(e));
+  }
+  ctx->used += bytes;
+  return TAGPU_OK;
+}
+
+void dev_free(tagpu_ctx* ctx, void* p, size_t bytes) {
+  if (!p) return;
+  cudaFreeAsync(p, ctx->stream);
+  ctx->used -= bytes;
+}
+
+}  // namespace
+
+tagpu_array::~tagpu_array() {
+  if (data) dev_free(ctx, data, bytes);
+}
+
+namespace {
+
+// Scoped device buffer on the context stream.
+struct DBuf {
+  tagpu_ctx* ctx = nullptr;
+  void* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  explicit DBuf(tagpu_ctx* c) : ctx(c) {}
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) dev_free(ctx, p, n);
+    p = nullptr;
+    n = 0;
+  }
+  tagpu_status alloc(size_t bytes) {
+    release();
+    tagpu_status st = dev_alloc(ctx, &p, bytes);
+    if (st == TAGPU_OK) n = bytes;
+    return st;
+  }
+  template <typename T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+template <typename T>
+tagpu_status upload_vec(tagpu_ctx* ctx, DBuf& b, const std::vector<T>& v) {
+  tagpu_status st = b.alloc(std::max<size_t>(1, v.size()) * sizeof(T));
+  if (st) return st;
+  if (!v.empty())
+    CUDA_TRY(ctx, cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+  return TAGPU_OK;
+}
+
+// recursive_outer_product (sparse_shape.h:106-131): split at ceil(d/2),
+// recurse, row-major outer product in float.
+std::vector<float> outer_sizes(const std::vector<std::vector<float>>& sv, size_t b, size_t e,
+                               bool inverse) {
+  if (e - b == 1) {
+    std::vector<float> r(sv[b].size());
+    for (size_t i = 0; i < r.size(); ++i) r[i] = inverse ? 1.0f / sv[b][i] : sv[b][i];
+    return r;
+  }
+  const size_t dim = e - b;
+  const size_t middle = (dim >> 1) + (dim & 1);
+  auto l = outer_sizes(sv, b, b + middle, inverse);
+  auto r = outer_sizes(sv, b + middle, e, inverse);
+  std::vector<float> out(l.size() * r.size());
+  for (size_t i = 0; i < l.size(); ++i)
+    for (size_t j = 0; j < r.size(); ++j) out[i * r.size() + j] = l[i] * r[j];
+  return out;
+}
+
+std::vector<std::vector<float>> size_vectors(const tagpu_array* a) {
+  std::vector<std::vector<float>> sv(a->rank);
+  for (int d = 0; d < a->rank; ++d) {
+    sv[d].resize(a->nt[d]);
+    for (int64_t i = 0; i < a->nt[d]; ++i) sv[d][i] = (float)(a->hm[d][i + 1] - a->hm[d][i]);
+  }
+  return sv;
+}
+
+// scale_tile_norms<InverseVolume, Screen> (sparse_shape.h:150-215)
+int64_t scale_norms(const tagpu_array* a, std::vector<float>& norms, float thr) {
+  auto sv = size_vectors(a);
+  int64_t zeros = 0;
+  if (a->rank == 1) {
+    for (size_t i = 0; i < norms.size(); ++i) {
+      norms[i] /= sv[0][i];
+      if (norms[i] < thr) {
+        norms[i] = 0.0f;
+        ++zeros;
+      }
+    }
+    return zeros;
+  }
+  if (a->rank == 0) return 0;
+  const size_t middle = (a->rank >> 1) + (a->rank & 1);
+  auto l = outer_sizes(sv, 0, middle, true);
+  auto r = outer_sizes(sv, middle, a->rank, true);
+  for (size_t i = 0; i < l.size(); ++i)
+    for (size_t j = 0; j < r.size(); ++j) {
+      float& v = norms[i * r.size() + j];
+      const float xy = l[i] * r[j];
+      v = v * xy;
+      if (v < thr) {
+        v = 0.0f;
+        ++zeros;
+      }
+    }
+  return zeros;
+}
+
+// Recompute offsets for a packed layout of the currently nonzero tiles.
+void pack_offsets(tagpu_array* a) {
+  const int64_t n = a->ntiles();
+  a->off.assign(n, -1);
+  int64_t pos = 0;
+  for (int64_t t = 0; t < n; ++t) {
+    if (a->tile_is_zero(t)) continue;
+    a->off[t] = pos;
+    pos += a->tile_volume(t);
+  }
+  a->elements = pos;
+}
+
+tagpu_status ensure_storage(tagpu_array* a) {
+  tagpu_ctx* ctx = a->ctx;
+  const size_t need = (size_t)a->elements * sizeof(double);
+  if (a->data && a->bytes == need) return TAGPU_OK;
+  if (a->data) dev_free(ctx, a->data, a->bytes);
+  a->data = nullptr;
+  a->bytes = 0;
+  if (need == 0) return TAGPU_OK;
+  void* p = nullptr;
+  tagpu_status st = dev_alloc(ctx, &p, need);
+  if (st) return st;
+  a->data = static_cast<double*>(p);
+  a->bytes = need;
+  return TAGPU_OK;
+}
+
+tagpu_array* new_array(tagpu_ctx* ctx, const std::vector<std::vector<int64_t>>& hm) {
+  auto* a = new tagpu_array;
+  a->ctx = ctx;
+  a->rank = (int)hm.size();
+  a->hm = hm;
+  a->nt.resize(a->rank);
+  for (int d = 0; d < a->rank; ++d) a->nt[d] = (int64_t)hm[d].size() - 1;
+  a->threshold = ctx->threshold;
+  pack_offsets(a);
+  return a;
+}
+
+// ---------------------------------------------------------------------------
+// index lists and the permutation optimizer
+// ---------------------------------------------------------------------------
+
+bool parse_indices(const char* s, std::vector<std::string>& out) {
+  out.clear();
+  if (!s) return false;
+  std::string cur;
+  auto flush = [&]() -> bool {
+    size_t b = cur.find_first_not_of(" \t"), e = cur.find_last_not_of(" \t");
+    if (b == std::string::npos) return false;
+    out.push_back(cur.substr(b, e - b + 1));
+    cur.clear();
+    return true;
+  };
+  bool any = false;
+  for (const char* p = s; *p; ++p) {
+    if (*p == ',') {
+      if (!flush()) return false;
+      any = true;
+    } else {
+      cur.push_back(*p);
+    }
+  }
+  if (cur.find_first_not_of(" \t") != std::string::npos) {
+    flush();
+  } else if (any) {
+    return false;  // trailing comma
+  }
+  for (size_t i = 0; i < out.size(); ++i)
+    for (size_t j = i + 1; j < out.size(); ++j)
+      if (out[i] == out[j]) return false;
+  return true;
+}
+
+int find_idx(const std::vector<std::string>& v, const std::string& x) {
+  for (size_t i = 0; i < v.size(); ++i)
+    if (v[i] == x) return (int)i;
+  return -1;
+}
+
+enum { IDENTITY = 1, MATRIX_TRANSPOSE = 2, GENERAL = 3 };
+
+// GEMMPermutationOptimizer::compute_index_list_contraction (permopt.h:258-376)
+struct PermOpt {
+  std::vector<std::string> left, right, result;
+  int lop = GENERAL, rop = GENERAL;
+};
+
+PermOpt permopt(const std::vector<std::string>& L, const std::vector<std::string>& R,
+                bool prefer_left) {
+  PermOpt o;
+  const size_t lr = L.size(), rr = R.size();
+  for (auto& v : L) {
+    if (find_idx(R, v) < 0) {
+      o.left.push_back(v);
+      o.result.push_back(v);
+    } else {
+      o.right.push_back(v);
+    }
+  }
+  const size_t inner = o.right.size(), lo = o.left.size(), ro = rr - inner;
+  if (inner == 0) {
+    for (auto& v : R) {
+      o.right.push_back(v);
+      o.result.push_back(v);
+    }
+    return o;
+  }
+  bool ordered = true, lnt = true, lt = true, rnt = true, rt = true;
+  const bool perm_left = lr < rr || (lr == rr && prefer_left);
+  for (size_t i = 0; i < rr; ++i) {
+    const std::string& idx = R[i];
+    const int jj = find_idx(L, idx);
+    if (jj < 0) {
+      o.right.push_back(idx);
+      o.result.push_back(idx);
+      continue;
+    }
+    const size_t j = (size_t)jj;
+    const size_t x = o.left.size() - lo;
+    ordered = ordered && o.right[x] == idx;
+    lnt = lnt && j >= lo;
+    lt = lt && j < inner;
+    rnt = rnt && i < inner;
+    rt = rt && i >= ro;
+    if (ordered) {
+      o.left.push_back(idx);
+    } else if (perm_left) {
+      o.left.push_back(idx);
+      o.right[x] = idx;
+      lnt = lt = false;
+    } else {
+      o.left.push_back(o.right[x]);
+      rnt = rt = false;
+    }
+  }
+  o.lop = lnt ? IDENTITY : (lt ? MATRIX_TRANSPOSE : GENERAL);
+  o.rop = rnt ? IDENTITY : (rt ? MATRIX_TRANSPOSE : GENERAL);
+  return o;
+}
+
+// perm with result dim perm[d] = argument dim d, mapping src order to dst
+std::vector<int> perm_between(const std::vector<std::string>& src,
+                              const std::vector<std::string>& dst) {
+  std::vector<int> p(src.size());
+  for (size_t d = 0; d < src.size(); ++d) p[d] = find_idx(dst, src[d]);
+  return p;
+}
+
+bool is_identity(const std::vector<int>& p) {
+  for (size_t d = 0; d < p.size(); ++d)
+    if (p[d] != (int)d) return false;
+  return true;
+}
+
+template <typename T>
+std::vector<T> permute_grid(const std::vector<T>& in, const std::vector<int64_t>& ext,
+                            const std::vector<int>& perm) {
+  const int r = (int)ext.size();
+  std::vector<T> out(in.size());
+  if (in.empty()) return out;
+  std::vector<int64_t> rext(r), rs(r), amap(r), idx(r, 0);
+  for (int d = 0; d < r; ++d) rext[perm[d]] = ext[d];
+  int64_t s = 1;
+  for (int d = r - 1; d >= 0; --d) {
+    rs[d] = s;
+    s *= rext[d];
+  }
+  for (int d = 0; d < r; ++d) amap[d] = rs[perm[d]];
+  int64_t ro = 0;
+  for (size_t o = 0; o < in.size(); ++o) {
+    out[ro] = in[o];
+    for (int d = r - 1; d >= 0; --d) {
+      ++idx[d];
+      ro += amap[d];
+      if (idx[d] < ext[d]) break;
+      ro -= amap[d] * idx[d];
+      idx[d] = 0;
+    }
+  }
+  return out;
+}
+
+struct EventTimer {
+  cudaEvent_t a, b;
+  cudaStream_t s;
+  explicit EventTimer(cudaStream_t st) : s(st) {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+  }
+  void stop() { cudaEventRecord(b, s); }
+  double ms() {
+    cudaEventSynchronize(b);
+    float f = 0;
+    cudaEventElapsedTime(&f, a, b);
+    return f;
+  }
+  ~EventTimer() {
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI: context
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+const char* tagpu_status_string(tagpu_status s) {
+  switch (s) {
+    case TAGPU_OK: return "ok";
+    case TAGPU_ERR_INVALID: return "invalid argument";
+    case TAGPU_ERR_UNSUPPORTED: return "unsupported";
+    case TAGPU_ERR_NOMEM: return "out of device memory";
+    case TAGPU_ERR_CUDA: return "CUDA error";
+    case TAGPU_ERR_TIMEOUT: return "timeout";
+    case TAGPU_ERR_REJECTED: return "rejected";
+    case TAGPU_ERR_NOT_READY: return "not ready";
+    case TAGPU_ERR_STATE: return "bad state";
+  }
+  return "unknown";
+}
+
+tagpu_status tagpu_init(const tagpu_config* cfg, tagpu_ctx** out) {
+  if (!out) return TAGPU_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return TAGPU_ERR_CUDA;
+  }
+  auto* ctx = new tagpu_ctx;
+  ctx->device = cfg ? cfg->device : 0;
+  ctx->budget = cfg ? cfg->hbm_budget_bytes : 0;
+  if (ctx->device < 0 || ctx->device >= ndev) {
+    delete ctx;
+    return TAGPU_ERR_INVALID;
+  }
+  if (cudaSetDevice(ctx->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return TAGPU_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  *out = ctx;
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_shutdown(tagpu_ctx* ctx) {
+  if (!ctx) return TAGPU_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return TAGPU_OK;
+}
+
+const char* tagpu_last_error(const tagpu_ctx* ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+tagpu_status tagpu_sync(tagpu_ctx* ctx) {
+  if (!ctx) return TAGPU_ERR_INVALID;
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return TAGPU_OK;
+}
+
+float tagpu_threshold_get(const tagpu_ctx* ctx) { return ctx ? ctx->threshold : 0.0f; }
+void tagpu_threshold_set(tagpu_ctx* ctx, float t) {
+  if (ctx) ctx->threshold = t;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI: arrays
+// ---------------------------------------------------------------------------
+
+tagpu_status tagpu_array_create(tagpu_ctx* ctx, int rank, const int64_t* ntiles,
+                                const int64_t* const* hashmarks, tagpu_array** out) {
+  if (!ctx || !out) return TAGPU_ERR_INVALID;
+  *out = nullptr;
+  if (rank < 0 || rank > 8 || (rank > 0 && (!ntiles || !hashmarks)))
+    return fail(ctx, TAGPU_ERR_INVALID, "array rank must be 0..8");
+  std::vector<std::vector<int64_t>> hm(rank);
+  for (int d = 0; d < rank; ++d) {
+    if (ntiles[d] < 0 || !hashmarks[d])
+      return fail(ctx, TAGPU_ERR_INVALID, "dimension %d: bad tiling", d);
+    hm[d].assign(hashmarks[d], hashmarks[d] + ntiles[d] + 1);
+    for (int64_t i = 0; i < ntiles[d]; ++i)
+      if (hm[d][i + 1] < hm[d][i])
+        return fail(ctx, TAGPU_ERR_INVALID, "dimension %d: hashmarks must not decrease", d);
+  }
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  std::unique_ptr<tagpu_array> a(new_array(ctx, hm));
+  tagpu_status st = ensure_storage(a.get());
+  if (st) return st;
+  *out = a.release();
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_array_destroy(tagpu_array* a) {
+  if (!a) return TAGPU_ERR_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(a->ctx->mu);
+  cudaSetDevice(a->ctx->device);
+  delete a;
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_array_set_shape(tagpu_array* a, const float* norms, int do_not_scale,
+                                   float threshold) {
+  if (!a) return TAGPU_ERR_INVALID;
+  tagpu_ctx* ctx = a->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  if (!norms) {
+    a->dense = true;
+    a->norms.clear();
+    a->zero_count = 0;
+  } else {
+    const float thr = threshold < 0 ? ctx->threshold : threshold;
+    a->dense = false;
+    a->norms.assign(norms, norms + a->ntiles());
+    a->threshold = thr;
+    if (!do_not_scale) {
+      a->zero_count = scale_norms(a, a->norms, thr);
+    } else {
+      a->zero_count = 0;
+      for (auto& v : a->norms)
+        if (v < thr) {
+          v = 0.0f;
+          ++a->zero_count;
+        }
+    }
+  }
+  pack_offsets(a);
+  return ensure_storage(a);
+}
+
+tagpu_status tagpu_array_upload(tagpu_array* a, const double* tiles, int64_t n) {
+  if (!a) return TAGPU_ERR_INVALID;
+  tagpu_ctx* ctx = a->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  if (n != a->elements)
+    return fail(ctx, TAGPU_ERR_INVALID, "upload: %lld elements given, array stores %lld",
+                (long long)n, (long long)a->elements);
+  if (n && !tiles) return fail(ctx, TAGPU_ERR_INVALID, "upload: null buffer");
+  // the packed host layout equals the device layout iff offsets are packed
+  pack_offsets(a);
+  tagpu_status st = ensure_storage(a);
+  if (st) return st;
+  if (n)
+    CUDA_TRY(ctx, cudaMemcpyAsync(a->data, tiles, n * sizeof(double), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_array_download(const tagpu_array* a, double* tiles, int64_t n) {
+  if (!a) return TAGPU_ERR_INVALID;
+  tagpu_ctx* ctx = a->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  if (n != a->elements)
+    return fail(ctx, TAGPU_ERR_INVALID, "download: buffer holds %lld elements, array %lld",
+                (long long)n, (long long)a->elements);
+  if (n && !tiles) return fail(ctx, TAGPU_ERR_INVALID, "download: null buffer");
+  if (n)
+    CUDA_TRY(ctx, cudaMemcpyAsync(tiles, a->data, n * sizeof(double), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_array_generate(tagpu_array* a, uint64_t seed, uint64_t stream, int kind,
+                                  const double* tile_scale, int compute_shape,
+                                  float threshold) {
+  if (!a) return TAGPU_ERR_INVALID;
+  tagpu_ctx* ctx = a->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  if (kind != 0 && kind != 1) return fail(ctx, TAGPU_ERR_INVALID, "generate: kind must be 0 or 1");
+  const int64_t n = a->ntiles();
+  // tiles present: scale != 0 (and, without compute_shape, nonzero in the shape)
+  std::vector<int64_t> lo, offs(1, 0), present;
+  std::vector<int32_t> ext;
+  std::vector<double> scale;
+  int64_t idx[8];
+  for (int64_t t = 0; t < n; ++t) {
+    const double sc = tile_scale ? tile_scale[t] : 1.0;
+    if (sc == 0.0) continue;
+    if (!compute_shape && a->tile_is_zero(t)) continue;
+    a->tile_index(t, idx);
+    for (int d = 0; d < a->rank; ++d) {
+      lo.push_back(a->hm[d][idx[d]] - a->hm[d][0]);
+      ext.push_back((int32_t)(a->hm[d][idx[d] + 1] - a->hm[d][idx[d]]));
+    }
+    scale.push_back(sc);
+    present.push_back(t);
+    offs.push_back(offs.back() + a->tile_volume(t));
+  }
+  const int64_t np = (int64_t)present.size();
+  // generate into a temporary packed buffer over the present tiles
+  DBuf dlo(ctx), dext(ctx), doff(ctx), dsc(ctx), dtmp(ctx);
+  tagpu_status st;
+  if ((st = upload_vec(ctx, dlo, lo)) || (st = upload_vec(ctx, dext, ext)) ||
+      (st = upload_vec(ctx, doff, offs)) || (st = upload_vec(ctx, dsc, scale)))
+    return st;
+  if ((st = dtmp.alloc(std::max<int64_t>(1, offs.back()) * sizeof(double)))) return st;
+  GenDesc g{};
+  g.rank = a->rank;
+  for (int d = 0; d < a->rank; ++d) g.gext[d] = a->hm[d].back() - a->hm[d][0];
+  g.seed = seed;
+  g.stream = stream;
+  g.kind = kind;
+  launch_generate(ctx->stream, g, np, dlo.as<int64_t>(), dext.as<int32_t>(),
+                  doff.as<int64_t>(), dsc.as<double>(), dtmp.as<double>());
+  CUDA_TRY(ctx, cudaGetLastError());
+  if (compute_shape) {
+    DBuf dn(ctx);
+    if ((st = dn.alloc(std::max<int64_t>(1, np) * sizeof(float)))) return st;
+    launch_tile_norms(ctx->stream, np, doff.as<int64_t>(), dtmp.as<double>(), dn.as<float>());
+    CUDA_TRY(ctx, cudaGetLastError());
+    std::vector<float> pn(np);
+    if (np)
+      CUDA_TRY(ctx, cudaMemcpyAsync(pn.data(), dn.p, np * sizeof(float), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    std::vector<float> norms(n, 0.0f);
+    for (int64_t x = 0; x < np; ++x) norms[present[x]] = pn[x];
+    const float thr = threshold < 0 ? ctx->threshold : threshold;
+    a->dense = false;
+    a->threshold = thr;
+    a->norms = norms;
+    a->zero_count = scale_norms(a, a->norms, thr);
+  }
+  pack_offsets(a);
+  if ((st = ensure_storage(a))) return st;
+  // move the present, nonzero tiles into place (contiguous runs when packed)
+  int64_t x = 0;
+  while (x < np) {
+    const int64_t t = present[x];
+    if (a->off[t] < 0) {
+      ++x;
+      continue;
+    }
+    int64_t y = x + 1;
+    while (y < np && a->off[present[y]] >= 0 &&
+           a->off[present[y]] == a->off[present[y - 1]] + (offs[y] - offs[y - 1]) &&
+           true)
+      ++y;
+    CUDA_TRY(ctx, cudaMemcpyAsync(a->data + a->off[t], dtmp.as<double>() + offs[x],
+                                  (offs[y] - offs[x]) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+    x = y;
+  }
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_array_get_info(const tagpu_array* a, tagpu_array_info* info) {
+  if (!a || !info) return TAGPU_ERR_INVALID;
+  info->rank = a->rank;
+  info->dense = a->dense ? 1 : 0;
+  info->ntiles_total = a->ntiles();
+  int64_t nz = 0;
+  for (auto o : a->off) nz += o >= 0;
+  info->nonzero_tiles = nz;
+  info->zero_tiles = a->dense ? 0 : a->zero_count;
+  info->elements = a->elements;
+  info->threshold = a->threshold;
+  info->device_bytes = a->bytes;
+  for (int d = 0; d < 8; ++d) info->ntiles[d] = d < a->rank ? a->nt[d] : 0;
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_array_get_norms(const tagpu_array* a, float* norms) {
+  if (!a || !norms) return TAGPU_ERR_INVALID;
+  const int64_t n = a->ntiles();
+  if (a->dense) {
+    for (int64_t t = 0; t < n; ++t) norms[t] = std::numeric_limits<float>::infinity();
+  } else {
+    std::copy(a->norms.begin(), a->norms.end(), norms);
+  }
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_array_get_tile_offsets(const tagpu_array* a, int64_t* offsets) {
+  if (!a || !offsets) return TAGPU_ERR_INVALID;
+  std::copy(a->off.begin(), a->off.end(), offsets);
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_array_get_hashmarks(const tagpu_array* a, int d, int64_t* hashmarks) {
+  if (!a || !hashmarks || d < 0 || d >= a->rank) return TAGPU_ERR_INVALID;
+  std::copy(a->hm[d].begin(), a->hm[d].end(), hashmarks);
+  return TAGPU_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// contraction: plan (host + kernels a/b, allocations) then enqueue (kernel d
+// and the result permutation, no host synchronisation, capturable)
+// ---------------------------------------------------------------------------
+
+namespace tagpu {
+
+// Tile permutation of a whole array, planned once and enqueued any number of
+// times (the descriptors live on the device).
+struct PermutePlan {
+  PermuteDesc pd{};
+  int64_t ntl = 0, nitems = 0;
+  DBuf ext, in_off, out_off, item_start;
+  explicit PermutePlan(tagpu_ctx* c) : ext(c), in_off(c), out_off(c), item_start(c) {}
+
+  // dst must already have the permuted tiling and packed offsets
+  tagpu_status build(const tagpu_array* a, const std::vector<int>& perm,
+                     const tagpu_array* dst) {
+    tagpu_ctx* ctx = a->ctx;
+    pd.rank = a->rank;
+    for (int d = 0; d < a->rank; ++d) pd.perm[d] = perm[d];
+    std::vector<int32_t> e32;
+    std::vector<int64_t> io, oo, is(1, 0);
+    int64_t idx[8], nidx[8], e[8];
+    for (int64_t t = 0; t < a->ntiles(); ++t) {
+      if (a->off[t] < 0) continue;
+      a->tile_index(t, idx);
+      for (int d = 0; d < a->rank; ++d) {
+        e[d] = a->hm[d][idx[d] + 1] - a->hm[d][idx[d]];
+        e32.push_back((int32_t)e[d]);
+        nidx[perm[d]] = idx[d];
+      }
+      int64_t no = 0;
+      for (int d = 0; d < a->rank; ++d) no = no * dst->nt[d] + nidx[d];
+      io.push_back(a->off[t]);
+      oo.push_back(dst->off[no]);
+      is.push_back(is.back() + (a->rank ? permute_items(pd, e) : 0));
+    }
+    ntl = (int64_t)io.size();
+    nitems = is.back();
+    tagpu_status st;
+    if ((st = upload_vec(ctx, ext, e32)) || (st = upload_vec(ctx, in_off, io)) ||
+        (st = upload_vec(ctx, out_off, oo)) || (st = upload_vec(ctx, item_start, is)))
+      return st;
+    return TAGPU_OK;
+  }
+  void enqueue(cudaStream_t s, const double* in, double* out) const {
+    if (ntl == 0) return;
+    if (pd.rank == 0) {
+      cudaMemcpyAsync(out, in, sizeof(double), cudaMemcpyDeviceToDevice, s);
+      return;
+    }
+    launch_permute(s, pd, ntl, ext.as<int32_t>(), in_off.as<int64_t>(), out_off.as<int64_t>(),
+                   item_start.as<int64_t>(), nitems, in, out);
+  }
+};
+
+// New array with the permuted tiling, norms and packed storage (no data).
+tagpu_array* permuted_layout(const tagpu_array* a, const std::vector<int>& perm) {
+  std::vector<std::vector<int64_t>> nhm(a->rank);
+  for (int d = 0; d < a->rank; ++d) nhm[perm[d]] = a->hm[d];
+  tagpu_array* r = new_array(a->ctx, nhm);
+  r->dense = a->dense;
+  r->threshold = a->threshold;
+  r->zero_count = a->zero_count;
+  if (!a->dense) r->norms = permute_grid(a->norms, a->nt, perm);
+  pack_offsets(r);
+  return r;
+}
+
+// Everything one contraction needs after planning.
+struct Contraction {
+  tagpu_ctx* ctx;
+  std::vector<std::string> ai, bi, ci;
+  PermOpt po;
+  int inner = 0, lorank = 0;
+  std::vector<int> lperm, rperm, cperm;
+  int64_t Mt = 1, Nt = 1, Kt = 1;
+  std::vector<int32_t> msz, nsz, ksz;
+  std::vector<float> kfl;               // k_sizes (float) for the shape gemm
+  std::vector<float> ln, rn;            // GEMM-order norms
+  float lthr = 0, rthr = 0, cthr = 0;
+  bool dense = false;
+  double alpha = 1.0;
+  int precision = TAGPU_PRECISION_FP64;
+  int slices = 6;
+  // operands in GEMM order
+  tagpu_array* Aop = nullptr;
+  tagpu_array* Bop = nullptr;
+  std::unique_ptr<tagpu_array> Aown, Bown;
+  int a_trans = 0, b_trans = 0;
+  std::vector<int64_t> aoff, boff;
+  // result in GEMM order (left outer, right outer) and in the target order
+  std::unique_ptr<tagpu_array> C, Cfinal;
+  std::unique_ptr<PermutePlan> post;
+  std::vector<float> cn;
+  int64_t zero_count = 0;
+  int64_t npairs = 0;
+  double flops = 0;
+  // device state
+  DBuf d_msz, d_nsz, d_ksz, d_aoff, d_boff, d_poff, d_kidx, d_coff;
+  std::vector<WorkItem> items;
+  GemmView view{};                      // fixed at plan time (device pointers)
+  double* post_in = nullptr;            // GEMM-order result
+  double* post_out = nullptr;           // target-order result
+  tagpu_contract_stats st{};
+  explicit Contraction(tagpu_ctx* c)
+      : ctx(c), d_msz(c), d_nsz(c), d_ksz(c), d_aoff(c), d_boff(c), d_poff(c), d_kidx(c),
+        d_coff(c) {}
+  tagpu_array* result() { return Cfinal ? Cfinal.get() : C.get(); }
+};
+
+}  // namespace tagpu
+
+namespace {
+
+std::vector<int32_t> fused_sizes(const tagpu_array* a, const std::vector<int>& dims) {
+  std::vector<int32_t> out(1, 1);
+  for (int d : dims) {
+    std::vector<int32_t> nxt;
+    nxt.reserve(out.size() * a->nt[d]);
+    for (auto x : out)
+      for (int64_t t = 0; t < a->nt[d]; ++t)
+        nxt.push_back(x * (int32_t)(a->hm[d][t + 1] - a->hm[d][t]));
+    out.swap(nxt);
+  }
+  return out;
+}
+
+// Parse, classify, choose layouts, GEMM-order sizes and norms.
+tagpu_status plan_contraction(Contraction& c, const char* c_idx, double alpha, tagpu_array* A,
+                              const char* a_idx, tagpu_array* B, const char* b_idx,
+                              float cthr) {
+  tagpu_ctx* ctx = c.ctx;
+  if (!parse_indices(a_idx, c.ai) || !parse_indices(b_idx, c.bi) || !parse_indices(c_idx, c.ci))
+    return fail(ctx, TAGPU_ERR_INVALID, "malformed index list");
+  if ((int)c.ai.size() != A->rank || (int)c.bi.size() != B->rank)
+    return fail(ctx, TAGPU_ERR_INVALID, "index list rank does not match the array rank");
+  if (A->dense != B->dense)
+    return fail(ctx, TAGPU_ERR_UNSUPPORTED, "dense and sparse arguments cannot be mixed");
+  // TensorProduct::Contraction: every target index is free in exactly one
+  // argument, every other index is shared by both arguments
+  for (auto& x : c.ci) {
+    const bool inA = find_idx(c.ai, x) >= 0, inB = find_idx(c.bi, x) >= 0;
+    if (inA == inB)
+      return fail(ctx, TAGPU_ERR_UNSUPPORTED,
+                  "index '%s' is not a free index of exactly one argument "
+                  "(Hadamard and general products are not on this path)", x.c_str());
+  }
+  for (auto& x : c.ai)
+    if (find_idx(c.bi, x) < 0 && find_idx(c.ci, x) < 0)
+      return fail(ctx, TAGPU_ERR_UNSUPPORTED, "index '%s' is summed over one argument only",
+                  x.c_str());
+  for (auto& x : c.bi)
+    if (find_idx(c.ai, x) < 0 && find_idx(c.ci, x) < 0)
+      return fail(ctx, TAGPU_ERR_UNSUPPORTED, "index '%s' is summed over one argument only",
+                  x.c_str());
+  c.po = permopt(c.ai, c.bi, true);
+  c.inner = (int)(c.ai.size() + c.bi.size() - c.po.result.size()) / 2;
+  c.lorank = (int)c.ai.size() - c.inner;
+  c.lperm = perm_between(c.ai, c.po.left);
+  c.rperm = perm_between(c.bi, c.po.right);
+  c.cperm = perm_between(c.po.result, c.ci);
+  for (int x = 0; x < c.inner; ++x) {
+    const std::string& v = c.po.left[c.lorank + x];
+    const int da = find_idx(c.ai, v), db = find_idx(c.bi, v);
+    if (A->hm[da] != B->hm[db])
+      return fail(ctx, TAGPU_ERR_INVALID,
+                  "the contracted dimensions '%s' of the arguments are not congruent",
+                  v.c_str());
+  }
+  std::vector<int> lo_dims, li_dims, ro_dims;
+  for (int x = 0; x < c.lorank; ++x) lo_dims.push_back(find_idx(c.ai, c.po.left[x]));
+  for (int x = 0; x < c.inner; ++x) li_dims.push_back(find_idx(c.ai, c.po.left[c.lorank + x]));
+  for (size_t x = c.inner; x < c.po.right.size(); ++x)
+    ro_dims.push_back(find_idx(c.bi, c.po.right[x]));
+  c.msz = fused_sizes(A, lo_dims);
+  c.ksz = fused_sizes(A, li_dims);
+  c.nsz = fused_sizes(B, ro_dims);
+  c.Mt = (int64_t)c.msz.size();
+  c.Kt = (int64_t)c.ksz.size();
+  c.Nt = (int64_t)c.nsz.size();
+  if (c.inner > 0) {
+    auto sv = size_vectors(A);
+    std::vector<std::vector<float>> ksv;
+    for (int d : li_dims) ksv.push_back(sv[d]);
+    c.kfl = outer_sizes(ksv, 0, ksv.size(), false);
+  }
+  c.dense = A->dense;
+  c.alpha = alpha;
+  c.cthr = cthr;
+  if (c.dense) {
+    c.ln.assign(c.Mt * c.Kt, 1.0f);
+    c.rn.assign(c.Kt * c.Nt, 1.0f);
+    c.lthr = c.rthr = 0.0f;
+  } else {
+    c.ln = permute_grid(A->norms, A->nt, c.lperm);
+    c.rn = permute_grid(B->norms, B->nt, c.rperm);
+    c.lthr = A->threshold;
+    c.rthr = B->threshold;
+  }
+  return TAGPU_OK;
+}
+
+// Steps (a) and (b) on the device.
+tagpu_status run_shape_and_pairs(Contraction& c) {
+  tagpu_ctx* ctx = c.ctx;
+  cudaStream_t s = ctx->stream;
+  const int64_t MN = c.Mt * c.Nt;
+  DBuf dL(ctx), dR(ctx), dK(ctx), dC(ctx), dz(ctx), dcnt(ctx), dfl(ctx);
+  tagpu_status e;
+  if ((e = upload_vec(ctx, dL, c.ln)) || (e = upload_vec(ctx, dR, c.rn)) ||
+      (e = upload_vec(ctx, dK, c.kfl)) || (e = upload_vec(ctx, c.d_msz, c.msz)) ||
+      (e = upload_vec(ctx, c.d_nsz, c.nsz)) || (e = upload_vec(ctx, c.d_ksz, c.ksz)))
+    return e;
+  if ((e = dC.alloc(std::max<int64_t>(1, MN) * sizeof(float))) ||
+      (e = dz.alloc(sizeof(unsigned long long))) ||
+      (e = dcnt.alloc(std::max<int64_t>(1, MN) * sizeof(int64_t))) ||
+      (e = dfl.alloc(sizeof(double))) || (e = c.d_poff.alloc((MN + 1) * sizeof(int64_t))))
+    return e;
+  CUDA_TRY(ctx, cudaMemsetAsync(dz.p, 0, sizeof(unsigned long long), s));
+  CUDA_TRY(ctx, cudaMemsetAsync(dfl.p, 0, sizeof(double), s));
+  const float af = (float)std::fabs(c.alpha);
+  {
+    EventTimer tm(s);
+    if (c.dense) {
+      // DenseShape::gemm (dense_shape.h:378-390): every result tile present
+      std::vector<float> ones(std::max<int64_t>(1, MN), 1.0f);
+      CUDA_TRY(ctx, cudaMemcpyAsync(dC.p, ones.data(), ones.size() * sizeof(float),
+                                    cudaMemcpyHostToDevice, s));
+      CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    } else if (c.inner > 0 && c.kfl.empty()) {
+      CUDA_TRY(ctx, cudaMemsetAsync(dC.p, 0, std::max<int64_t>(1, MN) * sizeof(float), s));
+      unsigned long long z = 0.0f < c.cthr ? (unsigned long long)MN : 0ull;
+      CUDA_TRY(ctx, cudaMemcpyAsync(dz.p, &z, sizeof(z), cudaMemcpyHostToDevice, s));
+      CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    } else {
+      launch_shape_gemm(s, c.Mt, c.Nt, c.inner > 0 ? c.Kt : 0, dL.as<float>(), dR.as<float>(),
+                        dK.as<float>(), af, c.cthr, dC.as<float>(),
+                        dz.as<unsigned long long>());
+    }
+    tm.stop();
+    CUDA_TRY(ctx, cudaGetLastError());
+    c.st.ms_shape = tm.ms();
+  }
+  c.cn.resize(MN);
+  unsigned long long zc = 0;
+  if (MN)
+    CUDA_TRY(ctx, cudaMemcpyAsync(c.cn.data(), dC.p, MN * sizeof(float), cudaMemcpyDeviceToHost,
+                                  s));
+  CUDA_TRY(ctx, cudaMemcpyAsync(&zc, dz.p, sizeof(zc), cudaMemcpyDeviceToHost, s));
+  {
+    EventTimer tm(s);
+    const float cthr = c.dense ? 0.0f : c.cthr;
+    launch_pair_count(s, c.Mt, c.Nt, c.Kt, dC.as<float>(), cthr, dL.as<float>(), c.lthr,
+                      dR.as<float>(), c.rthr, c.d_msz.as<int32_t>(), c.d_nsz.as<int32_t>(),
+                      c.d_ksz.as<int32_t>(), dcnt.as<int64_t>(), dfl.as<double>());
+    launch_exclusive_scan(s, dcnt.as<int64_t>(), MN, c.d_poff.as<int64_t>());
+    CUDA_TRY(ctx, cudaGetLastError());
+    int64_t np = 0;
+    CUDA_TRY(ctx, cudaMemcpyAsync(&np, c.d_poff.as<int64_t>() + MN, sizeof(int64_t),
+                                  cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(ctx, cudaMemcpyAsync(&c.flops, dfl.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    c.npairs = np;
+    if ((e = c.d_kidx.alloc(std::max<int64_t>(1, np) * sizeof(int32_t)))) return e;
+    launch_pair_emit(s, c.Mt, c.Nt, c.Kt, dC.as<float>(), cthr, dL.as<float>(), c.lthr,
+                     dR.as<float>(), c.rthr, c.d_poff.as<int64_t>(), c.d_kidx.as<int32_t>());
+    tm.stop();
+    CUDA_TRY(ctx, cudaGetLastError());
+    c.st.ms_pairs = tm.ms();
+  }
+  c.zero_count = c.dense ? 0 : (int64_t)zc;
+  return TAGPU_OK;
+}
+
+// Operands in GEMM order: explicit permutation for `general`, transposition
+// fused into the GEMM loaders otherwise (binary_engine.h:159-175).
+tagpu_status prepare_operands(Contraction& c, tagpu_array* A, tagpu_array* B) {
+  tagpu_ctx* ctx = c.ctx;
+  tagpu_status e;
+  auto explicit_permute = [&](tagpu_array* X, const std::vector<int>& perm,
+                              std::unique_ptr<tagpu_array>& own) -> tagpu_status {
+    own.reset(permuted_layout(X, perm));
+    tagpu_status st = ensure_storage(own.get());
+    if (st) return st;
+    PermutePlan pp(ctx);
+    if ((st = pp.build(X, perm, own.get()))) return st;
+    EventTimer tm(ctx->stream);
+    pp.enqueue(ctx->stream, X->data, own->data);
+    tm.stop();
+    CUDA_TRY(ctx, cudaGetLastError());
+    c.st.ms_permute += tm.ms();
+    return TAGPU_OK;
+  };
+  if (c.po.lop == GENERAL && !is_identity(c.lperm)) {
+    if ((e = explicit_permute(A, c.lperm, c.Aown))) return e;
+    c.Aop = c.Aown.get();
+    c.a_trans = 0;
+  } else {
+    c.Aop = A;
+    c.a_trans = (c.po.lop == MATRIX_TRANSPOSE && !is_identity(c.lperm)) ? 1 : 0;
+  }
+  if (c.po.rop == GENERAL && !is_identity(c.rperm)) {
+    if ((e = explicit_permute(B, c.rperm, c.Bown))) return e;
+    c.Bop = c.Bown.get();
+    c.b_trans = 0;
+  } else {
+    c.Bop = B;
+    c.b_trans = (c.po.rop == MATRIX_TRANSPOSE && !is_identity(c.rperm)) ? 1 : 0;
+  }
+  c.aoff.assign(c.Mt * c.Kt, -1);
+  c.boff.assign(c.Kt * c.Nt, -1);
+  if (c.inner == 0) {
+    for (int64_t m = 0; m < c.Mt; ++m) c.aoff[m] = c.Aop->off[m];
+    for (int64_t n = 0; n < c.Nt; ++n) c.boff[n] = c.Bop->off[n];
+    c.a_trans = c.b_trans = 0;
+  } else {
+    for (int64_t m = 0; m < c.Mt; ++m)
+      for (int64_t k = 0; k < c.Kt; ++k)
+        c.aoff[m * c.Kt + k] = c.Aop->off[c.a_trans ? k * c.Mt + m : m * c.Kt + k];
+    for (int64_t k = 0; k < c.Kt; ++k)
+      for (int64_t n = 0; n < c.Nt; ++n)
+        c.boff[k * c.Nt + n] = c.Bop->off[c.b_trans ? n * c.Kt + k : k * c.Nt + n];
+  }
+  if ((e = upload_vec(ctx, c.d_aoff, c.aoff)) || (e = upload_vec(ctx, c.d_boff, c.boff)))
+    return e;
+  return TAGPU_OK;
+}
+
+// Result arrays: GEMM order (written by kernel d) and, when the target order
+// differs, the permuted target (contract_reduce.h:370-381).
+tagpu_status make_result(Contraction& c, tagpu_array* A, tagpu_array* B) {
+  tagpu_ctx* ctx = c.ctx;
+  std::vector<std::vector<int64_t>> hm;
+  for (int x = 0; x < c.lorank; ++x) hm.push_back(A->hm[find_idx(c.ai, c.po.left[x])]);
+  for (size_t x = c.inner; x < c.po.right.size(); ++x)
+    hm.push_back(B->hm[find_idx(c.bi, c.po.right[x])]);
+  c.C.reset(new_array(ctx, hm));
+  tagpu_array* C = c.C.get();
+  C->dense = c.dense;
+  C->threshold = c.cthr;
+  if (!c.dense) {
+    C->norms = c.cn;
+    C->norms.resize(C->ntiles(), 0.0f);
+  }
+  C->zero_count = c.zero_count;
+  pack_offsets(C);
+  tagpu_status e = ensure_storage(C);
+  if (e) return e;
+  std::vector<int64_t> coff(c.Mt * c.Nt, -1);
+  for (int64_t t = 0; t < (int64_t)coff.size() && t < C->ntiles(); ++t) coff[t] = C->off[t];
+  if ((e = upload_vec(ctx, c.d_coff, coff))) return e;
+  if (!is_identity(c.cperm)) {
+    c.Cfinal.reset(permuted_layout(C, c.cperm));
+    if ((e = ensure_storage(c.Cfinal.get()))) return e;
+    c.post.reset(new PermutePlan(ctx));
+    if ((e = c.post->build(C, c.cperm, c.Cfinal.get()))) return e;
+  }
+  return TAGPU_OK;
+}
+
+GemmView gemm_view(Contraction& c) {
+  GemmView v{};
+  v.Mt = c.Mt;
+  v.Nt = c.Nt;
+  v.Kt = c.Kt;
+  v.msz = c.d_msz.as<int32_t>();
+  v.nsz = c.d_nsz.as<int32_t>();
+  v.ksz = c.d_ksz.as<int32_t>();
+  v.A = c.Aop->data;
+  v.aoff = c.d_aoff.as<int64_t>();
+  v.a_trans = c.a_trans;
+  v.B = c.Bop->data;
+  v.boff = c.d_boff.as<int64_t>();
+  v.b_trans = c.b_trans;
+  v.poff = c.d_poff.as<int64_t>();
+  v.kidx = c.d_kidx.as<int32_t>();
+  v.alpha = c.alpha;
+  v.C = c.C->data;
+  v.coff = c.d_coff.as<int64_t>();
+  return v;
+}
+
+tagpu_status build_dmma_items(Contraction& c, int32_t view) {
+  c.items.clear();
+  for (int64_t t = 0; t < c.Mt * c.Nt; ++t) {
+    if (c.C->off[t] < 0) continue;
+    const int64_t i = t / c.Nt, j = t % c.Nt;
+    const int64_t rbs = (c.msz[i] + 63) / 64, cbs = (c.nsz[j] + 63) / 64;
+    if (rbs > 32767 || cbs > 32767)
+      return fail(c.ctx, TAGPU_ERR_UNSUPPORTED, "fused tile extent above 2097088");
+    for (int64_t rb = 0; rb < rbs; ++rb)
+      for (int64_t cb = 0; cb < cbs; ++cb)
+        c.items.push_back(WorkItem{t, view, (int16_t)rb, (int16_t)cb});
+  }
+  return TAGPU_OK;
+}
+
+// Full planning of one contraction.
+tagpu_status plan_all(Contraction& c, const char* c_idx, double alpha, tagpu_array* A,
+                      const char* a_idx, tagpu_array* B, const char* b_idx,
+                      const tagpu_contract_opts* opts) {
+  tagpu_ctx* ctx = c.ctx;
+  c.precision = opts ? opts->precision : TAGPU_PRECISION_FP64;
+  c.slices = opts && opts->slices > 0 ? opts->slices : 6;
+  const float cthr = opts && opts->threshold >= 0 ? opts->threshold : ctx->threshold;
+  if (c.precision != TAGPU_PRECISION_FP64 && c.precision != TAGPU_PRECISION_OZAKI)
+    return fail(ctx, TAGPU_ERR_INVALID, "unknown precision %d", c.precision);
+  if (c.precision == TAGPU_PRECISION_OZAKI && (c.slices < 2 || c.slices > 8))
+    return fail(ctx, TAGPU_ERR_INVALID, "slices must be 2..8");
+  tagpu_status e;
+  if ((e = plan_contraction(c, c_idx, alpha, A, a_idx, B, b_idx, cthr))) return e;
+  if ((e = run_shape_and_pairs(c))) return e;
+  if ((e = make_result(c, A, B))) return e;
+  if ((e = prepare_operands(c, A, B))) return e;
+  c.view = gemm_view(c);
+  if ((e = build_dmma_items(c, 0))) return e;
+  if (c.post) {
+    c.post_in = c.C->data;
+    c.post_out = c.Cfinal->data;
+  }
+  return TAGPU_OK;
+}
+
+void fill_stats(Contraction& c) {
+  tagpu_contract_stats& st = c.st;
+  st.result_tiles = c.Mt * c.Nt;
+  int64_t nz = 0;
+  for (auto o : c.result()->off) nz += o >= 0;
+  st.nonzero_result_tiles = nz;
+  st.zero_tiles = c.zero_count;
+  st.pairs = c.npairs;
+  st.flops = c.flops;
+  st.left_permtype = c.po.lop;
+  st.right_permtype = c.po.rop;
+  st.precision = c.precision;
+  st.slices = c.precision == TAGPU_PRECISION_OZAKI ? c.slices : 0;
+}
+
+// Move the contents of `src` into the caller-visible handle `dst`.
+void move_into(tagpu_array* dst, tagpu_array* src) {
+  if (dst->data) dev_free(dst->ctx, dst->data, dst->bytes);
+  dst->rank = src->rank;
+  dst->hm = std::move(src->hm);
+  dst->nt = std::move(src->nt);
+  dst->dense = src->dense;
+  dst->norms = std::move(src->norms);
+  dst->threshold = src->threshold;
+  dst->zero_count = src->zero_count;
+  dst->off = std::move(src->off);
+  dst->elements = src->elements;
+  dst->data = src->data;
+  dst->bytes = src->bytes;
+  src->data = nullptr;
+  src->bytes = 0;
+}
+
+}  // namespace
+
+namespace tagpu {
+
+// Kernel (d) and the post-permutation for a set of planned contractions;
+// no host synchronisation, so the sequence can be captured in a graph.
+tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, DBuf& d_views,
+                           DBuf& d_items, bool upload) {
+  std::vector<GemmView> views;
+  std::vector<WorkItem> items;
+  for (auto* c : cs) {
+    if (c->view.C == nullptr) continue;
+    if (c->precision == TAGPU_PRECISION_FP64 || c->npairs == 0) {
+      const int32_t vid = (int32_t)views.size();
+      views.push_back(c->view);
+      for (WorkItem w : c->items) {
+        w.view = vid;
+        items.push_back(w);
+      }
+    }
+  }
+  if (upload) {
+    tagpu_status e;
+    if ((e = upload_vec(ctx, d_views, views)) || (e = upload_vec(ctx, d_items, items))) return e;
+  }
+  for (auto* c : cs) {
+    if (c->view.C == nullptr || c->precision == TAGPU_PRECISION_FP64 || c->npairs == 0) continue;
+    const GemmView& v = c->view;
+    size_t scratch = 0;
+    std::string err;
+    tagpu_status e = ozaki_run(ctx->stream, v, c->slices, ctx->sm_count, &scratch,
+                               &c->st.ms_split, &c->st.ms_gemm, &c->st.gemm_blocks, &err);
+    if (e) return fail(ctx, e, "%s", err.c_str());
+    c->st.gemm_launches += 3;
+  }
+  if (!items.empty()) {
+    launch_dmma_gemm(ctx->stream, d_views.as<GemmView>(), d_items.as<WorkItem>(),
+                     (int64_t)items.size(), ctx->sm_count);
+    for (auto* c : cs) {
+      if (c->precision != TAGPU_PRECISION_FP64 && c->npairs > 0) continue;
+      c->st.gemm_blocks = (int64_t)c->items.size();
+      c->st.gemm_launches = c->items.empty() ? 0 : 1;
+    }
+  }
+  for (auto* c : cs)
+    if (c->post) c->post->enqueue(ctx->stream, c->post_in, c->post_out);
+  CUDA_TRY(ctx, cudaGetLastError());
+  return TAGPU_OK;
+}
+
+tagpu_status contract_impl(tagpu_ctx* ctx, const char* c_idx, double alpha, tagpu_array* A,
+                           const char* a_idx, tagpu_array* B, const char* b_idx,
+                           const tagpu_contract_opts* opts, tagpu_array** out,
+                           tagpu_contract_stats* stats) {
+  const auto t0 = std::chrono::steady_clock::now();
+  Contraction c(ctx);
+  tagpu_status e = plan_all(c, c_idx, alpha, A, a_idx, B, b_idx, opts);
+  if (e) return e;
+  DBuf dv(ctx), di(ctx);
+  std::vector<Contraction*> cs{&c};
+  {
+    EventTimer tm(ctx->stream);
+    if ((e = enqueue_gemms(ctx, cs, dv, di, true))) return e;
+    tm.stop();
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (c.precision == TAGPU_PRECISION_FP64 || c.npairs == 0) c.st.ms_gemm = tm.ms();
+  }
+  fill_stats(c);
+  c.st.ms_total =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (stats) *stats = c.st;
+  *out = c.Cfinal ? c.Cfinal.release() : c.C.release();
+  return TAGPU_OK;
+}
+
+}  // namespace tagpu
+
+// ---------------------------------------------------------------------------
+// batches: many contractions, one persistent GEMM launch, captured in a graph
+// ---------------------------------------------------------------------------
+
+struct tagpu_batch {
+  tagpu_ctx* ctx;
+  struct Entry {
+    std::string c, a, b;
+    double alpha;
+    tagpu_array *A, *B, *C;
+    tagpu_contract_opts opts;
+    std::unique_ptr<Contraction> plan;
+  };
+  std::vector<Entry> entries;
+  bool planned = false;
+  DBuf d_views, d_items;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  tagpu_contract_stats stats{};
+  explicit tagpu_batch(tagpu_ctx* c) : ctx(c), d_views(c), d_items(c) {}
+  ~tagpu_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+};
+
+extern "C" {
+
+tagpu_status tagpu_contract(tagpu_ctx* ctx, const char* c_idx, double alpha, tagpu_array* A,
+                            const char* a_idx, tagpu_array* B, const char* b_idx,
+                            const tagpu_contract_opts* opts, tagpu_array** c) {
+  if (!ctx || !A || !B || !c) return ctx ? fail(ctx, TAGPU_ERR_INVALID, "null argument")
+                                         : TAGPU_ERR_INVALID;
+  if (A->ctx != ctx || B->ctx != ctx)
+    return fail(ctx, TAGPU_ERR_INVALID, "arrays belong to another context");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  *c = nullptr;
+  return contract_impl(ctx, c_idx, alpha, A, a_idx, B, b_idx, opts, c, &ctx->last);
+}
+
+tagpu_status tagpu_batch_create(tagpu_ctx* ctx, tagpu_batch** out) {
+  if (!ctx || !out) return TAGPU_ERR_INVALID;
+  *out = new tagpu_batch(ctx);
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_batch_add(tagpu_batch* b, const char* c_idx, double alpha, tagpu_array* A,
+                             const char* a_idx, tagpu_array* B, const char* b_idx,
+                             const tagpu_contract_opts* opts, tagpu_array** c) {
+  if (!b || !A || !B || !c || !c_idx || !a_idx || !b_idx) return TAGPU_ERR_INVALID;
+  tagpu_ctx* ctx = b->ctx;
+  if (b->planned) return fail(ctx, TAGPU_ERR_STATE, "batch already ran; create a new one");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  tagpu_batch::Entry e;
+  e.c = c_idx;
+  e.a = a_idx;
+  e.b = b_idx;
+  e.alpha = alpha;
+  e.A = A;
+  e.B = B;
+  e.opts = opts ? *opts : tagpu_contract_opts{TAGPU_PRECISION_FP64, 0, -1.0f};
+  e.C = new_array(ctx, {});
+  b->entries.push_back(std::move(e));
+  *c = b->entries.back().C;
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_batch_run(tagpu_batch* b) {
+  if (!b) return TAGPU_ERR_INVALID;
+  tagpu_ctx* ctx = b->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  const auto t0 = std::chrono::steady_clock::now();
+  tagpu_status e;
+  if (!b->planned) {
+    std::vector<Contraction*> cs;
+    for (auto& en : b->entries) {
+      en.plan.reset(new Contraction(ctx));
+      if ((e = plan_all(*en.plan, en.c.c_str(), en.alpha, en.A, en.a.c_str(), en.B,
+                        en.b.c_str(), &en.opts)))
+        return e;
+      cs.push_back(en.plan.get());
+    }
+    // hand the result storage to the caller-visible handles now: the device
+    // pointers the graph captures stay valid as long as the handles live
+    for (auto& en : b->entries) {
+      Contraction& c = *en.plan;
+      fill_stats(c);
+    }
+    bool has_ozaki = false;
+    for (auto* c : cs) has_ozaki |= c->precision == TAGPU_PRECISION_OZAKI && c->npairs > 0;
+    if (has_ozaki) {
+      // the emulated form plans its own scratch; run it eagerly
+      if ((e = enqueue_gemms(ctx, cs, b->d_views, b->d_items, true))) return e;
+    } else {
+      // upload views/items first (outside capture), then capture the launches
+      if ((e = enqueue_gemms(ctx, cs, b->d_views, b->d_items, true))) return e;
+      CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      e = enqueue_gemms(ctx, cs, b->d_views, b->d_items, false);
+      cudaGraph_t g = nullptr;
+      cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+      if (e) return e;
+      if (ce != cudaSuccess) return fail(ctx, TAGPU_ERR_CUDA, "graph capture failed: %s",
+                                         cudaGetErrorString(ce));
+      b->graph = g;
+      CUDA_TRY(ctx, cudaGraphInstantiate(&b->exec, g, 0));
+    }
+    // results move into the caller-visible handles; the captured launches
+    // keep writing the same device buffers, so a result handle must outlive
+    // the runs of its batch
+    for (auto& en : b->entries) move_into(en.C, en.plan->result());
+    b->planned = true;
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  } else {
+    if (b->exec) {
+      CUDA_TRY(ctx, cudaGraphLaunch(b->exec, ctx->stream));
+    } else {
+      std::vector<Contraction*> cs;
+      for (auto& en : b->entries) cs.push_back(en.plan.get());
+      if ((e = enqueue_gemms(ctx, cs, b->d_views, b->d_items, false))) return e;
+    }
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  tagpu_contract_stats& s = b->stats;
+  s = tagpu_contract_stats{};
+  for (auto& en : b->entries) {
+    const auto& c = en.plan->st;
+    s.result_tiles += c.result_tiles;
+    s.nonzero_result_tiles += c.nonzero_result_tiles;
+    s.zero_tiles += c.zero_tiles;
+    s.pairs += c.pairs;
+    s.flops += c.flops;
+    s.ms_shape += c.ms_shape;
+    s.ms_pairs += c.ms_pairs;
+    s.ms_permute += c.ms_permute;
+    s.ms_split += c.ms_split;
+    s.gemm_blocks += c.gemm_blocks;
+  }
+  s.gemm_launches = b->exec ? 1 : 0;
+  s.ms_total =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_batch_stats(const tagpu_batch* b, tagpu_contract_stats* st) {
+  if (!b || !st) return TAGPU_ERR_INVALID;
+  *st = b->stats;
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_batch_destroy(tagpu_batch* b) {
+  if (!b) return TAGPU_ERR_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(b->ctx->mu);
+  cudaSetDevice(b->ctx->device);
+  cudaStreamSynchronize(b->ctx->stream);
+  delete b;
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_last_stats(const tagpu_ctx* ctx, tagpu_contract_stats* st) {
+  if (!ctx || !st) return TAGPU_ERR_INVALID;
+  *st = ctx->last;
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_shape_gemm(tagpu_ctx* ctx, int64_t M, int64_t N, int64_t K,
+                              const float* left, const float* right, const float* k_sizes,
+                              double factor, float threshold, float* result,
+                              int64_t* zero_count) {
+  if (!ctx || M < 0 || N < 0 || K < 0 || (M * N != 0 && !result))
+    return ctx ? fail(ctx, TAGPU_ERR_INVALID, "shape_gemm: bad arguments") : TAGPU_ERR_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  const bool outer = k_sizes == nullptr;
+  const int64_t Kl = outer ? 1 : K;
+  std::vector<float> l(left, left + M * Kl), r(right, right + Kl * N);
+  std::vector<float> ks;
+  if (!outer) ks.assign(k_sizes, k_sizes + K);
+  DBuf dL(ctx), dR(ctx), dK(ctx), dC(ctx), dz(ctx);
+  tagpu_status e;
+  if ((e = upload_vec(ctx, dL, l)) || (e = upload_vec(ctx, dR, r)) || (e = upload_vec(ctx, dK, ks)) ||
+      (e = dC.alloc(std::max<int64_t>(1, M * N) * sizeof(float))) ||
+      (e = dz.alloc(sizeof(unsigned long long))))
+    return e;
+  CUDA_TRY(ctx, cudaMemsetAsync(dz.p, 0, sizeof(unsigned long long), ctx->stream));
+  if (!outer && K == 0) {
+    CUDA_TRY(ctx, cudaMemsetAsync(dC.p, 0, std::max<int64_t>(1, M * N) * sizeof(float),
+                                  ctx->stream));
+    unsigned long long z = (unsigned long long)(M * N);
+    CUDA_TRY(ctx, cudaMemcpyAsync(dz.p, &z, sizeof(z), cudaMemcpyHostToDevice, ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    // 0 < threshold for any positive threshold: every tile is zero
+    if (!(0.0f < threshold)) {
+      z = 0;
+      CUDA_TRY(ctx, cudaMemcpyAsync(dz.p, &z, sizeof(z), cudaMemcpyHostToDevice, ctx->stream));
+    }
+  } else {
+    launch_shape_gemm(ctx->stream, M, N, outer ? 0 : K, dL.as<float>(), dR.as<float>(),
+                      dK.as<float>(), (float)std::fabs(factor), threshold, dC.as<float>(),
+                      dz.as<unsigned long long>());
+    CUDA_TRY(ctx, cudaGetLastError());
+  }
+  unsigned long long z = 0;
+  if (M * N != 0)
+    CUDA_TRY(ctx, cudaMemcpyAsync(result, dC.p, M * N * sizeof(float), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+  CUDA_TRY(ctx, cudaMemcpyAsync(&z, dz.p, sizeof(z), cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (zero_count) *zero_count = (int64_t)z;
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_pair_list(tagpu_ctx* ctx, int64_t M, int64_t N, int64_t K,
+                             const float* cnorm, float c_thr, const float* lnorm, float l_thr,
+                             const float* rnorm, float r_thr, int64_t* offsets, int32_t* kidx,
+                             int64_t kidx_cap, int64_t* npairs) {
+  if (!ctx || M < 0 || N < 0 || K < 0 || !offsets)
+    return ctx ? fail(ctx, TAGPU_ERR_INVALID, "pair_list: bad arguments") : TAGPU_ERR_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  const int64_t MN = M * N;
+  std::vector<float> c(cnorm, cnorm + MN), l(lnorm, lnorm + M * K), r(rnorm, rnorm + K * N);
+  std::vector<int32_t> ones_m(std::max<int64_t>(1, M), 1), ones_n(std::max<int64_t>(1, N), 1),
+      ones_k(std::max<int64_t>(1, K), 1);
+  DBuf dC(ctx), dL(ctx), dR(ctx), dm(ctx), dn(ctx), dk(ctx), dcnt(ctx), doff(ctx), dki(ctx),
+      dfl(ctx);
+  tagpu_status e;
+  if ((e = upload_vec(ctx, dC, c)) || (e = upload_vec(ctx, dL, l)) || (e = upload_vec(ctx, dR, r)) ||
+      (e = upload_vec(ctx, dm, ones_m)) || (e = upload_vec(ctx, dn, ones_n)) ||
+      (e = upload_vec(ctx, dk, ones_k)) ||
+      (e = dcnt.alloc(std::max<int64_t>(1, MN) * sizeof(int64_t))) ||
+      (e = doff.alloc((MN + 1) * sizeof(int64_t))) || (e = dfl.alloc(sizeof(double))))
+    return e;
+  CUDA_TRY(ctx, cudaMemsetAsync(dfl.p, 0, sizeof(double), ctx->stream));
+  launch_pair_count(ctx->stream, M, N, K, dC.as<float>(), c_thr, dL.as<float>(), l_thr,
+                    dR.as<float>(), r_thr, dm.as<int32_t>(), dn.as<int32_t>(), dk.as<int32_t>(),
+                    dcnt.as<int64_t>(), dfl.as<double>());
+  launch_exclusive_scan(ctx->stream, dcnt.as<int64_t>(), MN, doff.as<int64_t>());
+  CUDA_TRY(ctx, cudaGetLastError());
+  CUDA_TRY(ctx, cudaMemcpyAsync(offsets, doff.p, (MN + 1) * sizeof(int64_t),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  const int64_t np = offsets[MN];
+  if (npairs) *npairs = np;
+  if (kidx) {
+    if (kidx_cap < np) return fail(ctx, TAGPU_ERR_INVALID, "pair_list: kidx capacity too small");
+    if ((e = dki.alloc(std::max<int64_t>(1, np) * sizeof(int32_t)))) return e;
+    launch_pair_emit(ctx->stream, M, N, K, dC.as<float>(), c_thr, dL.as<float>(), l_thr,
+                     dR.as<float>(), r_thr, doff.as<int64_t>(), dki.as<int32_t>());
+    CUDA_TRY(ctx, cudaGetLastError());
+    if (np)
+      CUDA_TRY(ctx, cudaMemcpyAsync(kidx, dki.p, np * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_permute(tagpu_ctx* ctx, int rank, const int64_t* extents, const int32_t* perm,
+                           const double* in, double* out) {
+  if (!ctx || rank < 1 || rank > 8 || !extents || !perm)
+    return ctx ? fail(ctx, TAGPU_ERR_INVALID, "permute: bad arguments") : TAGPU_ERR_INVALID;
+  std::vector<bool> seen(rank, false);
+  for (int d = 0; d < rank; ++d) {
+    if (perm[d] < 0 || perm[d] >= rank || seen[perm[d]])
+      return fail(ctx, TAGPU_ERR_INVALID, "permute: not a permutation");
+    seen[perm[d]] = true;
+  }
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  int64_t vol = 1;
+  for (int d = 0; d < rank; ++d) vol *= extents[d];
+  if (vol == 0) return TAGPU_OK;
+  if (!in || !out) return fail(ctx, TAGPU_ERR_INVALID, "permute: null buffer");
+  PermuteDesc pd{};
+  pd.rank = rank;
+  for (int d = 0; d < rank; ++d) pd.perm[d] = perm[d];
+  std::vector<int32_t> ext(extents, extents + rank);
+  std::vector<int64_t> zero(1, 0), items = {0, permute_items(pd, extents)};
+  DBuf dext(ctx), dio(ctx), dis(ctx), din(ctx), dout(ctx);
+  tagpu_status e;
+  if ((e = upload_vec(ctx, dext, ext)) || (e = upload_vec(ctx, dio, zero)) ||
+      (e = upload_vec(ctx, dis, items)) || (e = din.alloc(vol * sizeof(double))) ||
+      (e = dout.alloc(vol * sizeof(double))))
+    return e;
+  CUDA_TRY(ctx, cudaMemcpyAsync(din.p, in, vol * sizeof(double), cudaMemcpyHostToDevice,
+                                ctx->stream));
+  launch_permute(ctx->stream, pd, 1, dext.as<int32_t>(), dio.as<int64_t>(), dio.as<int64_t>(),
+                 dis.as<int64_t>(), items[1], din.as<double>(), dout.as<double>());
+  CUDA_TRY(ctx, cudaGetLastError());
+  CUDA_TRY(ctx, cudaMemcpyAsync(out, dout.p, vol * sizeof(double), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return TAGPU_OK;
+}
+
+}  // extern "C"
