@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""Benchmark of the block-sparse contraction path on one GB300.
+
+Workload (the block-sparse matrix product TSpArrayD, N = 16384): tile sizes
+drawn uniformly from [48, 256] per dimension (seeded; the last tile absorbs a
+remainder below 48), block (I, J) filled with uniform[-1, 1) entries scaled by
+exp(-|I-J|/4) and absent when that factor is below 1e-10, SparseShape
+threshold 1e-8 for the operands and the result.  Synthetic data generated on
+the device with the counter-based generator.
+
+A step is one C("i,j") = A("i,k") * B("k,j") through tagpu_contract with the
+operands resident in HBM: screening, pair list, and the emulated-FP64 GEMM
+(exact bf16 digit slices on tcgen05) that writes the result tiles.  The metric
+is nonzero-block TFLOP/s = 2 * sum over the tile-pair list of m*k*n per
+second.  The operands (~1.7 GB each) are far larger than L2, so no flush is
+needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "nonzero-block TFLOP/s at <=1e-12 rel err, emulated vs plain FP64; p50/p99 latency"
+SLICE_PAIRS = {s: s * (s + 1) // 2 for s in range(2, 9)}
+
+
+def workload(n=16384, seed=0, lo=48, hi=256, decay=4.0, cut=1e-10):
+    rng = np.random.default_rng(seed)
+    h = [0]
+    while h[-1] < n:
+        rem = n - h[-1]
+        s = int(rng.integers(lo, hi + 1))
+        if rem - s < lo:
+            s = rem
+        h.append(h[-1] + s)
+    nt = len(h) - 1
+    I, J = np.meshgrid(np.arange(nt), np.arange(nt), indexing="ij")
+    scale = np.exp(-np.abs(I - J) / decay)
+    scale[scale < cut] = 0.0
+    return h, scale
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device):
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(device),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 8:
+                    continue
+                try:
+                    sm.append(float(parts[0]))
+                    smax.append(float(parts[1]))
+                except ValueError:
+                    continue
+                for name, v in zip(names, parts[4:8]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_sample(A_t, B_t, h, scale, seconds, threads, seed=0):
+    """Oracle (vendor-BLAS dgemm per tile pair) on a bounded sample of result
+    tiles of the same contraction; returns (TFLOP/s, sample description)."""
+    import oracle as O
+    fn = O.openblas_dgemm()
+    thr = 1e-8
+    nt = len(h) - 1
+    sizes = np.diff(np.asarray(h))
+    An, Bn = A_t["norms"].reshape(nt, nt), B_t["norms"].reshape(nt, nt)
+    ks = sizes.astype(np.float32)
+    cn, _ = O.shape_gemm(An, Bn, ks, 1.0, thr)
+    offs, kidx = O.pairs(cn, thr, An, thr, Bn, thr)
+    # per result tile flops
+    tile_fl = np.zeros(nt * nt)
+    for t in range(nt * nt):
+        ks_t = kidx[offs[t]:offs[t + 1]]
+        if len(ks_t):
+            tile_fl[t] = 2.0 * sizes[t // nt] * sizes[t % nt] * sizes[ks_t].sum()
+    rng = np.random.default_rng(seed)
+    cand = np.flatnonzero(tile_fl > 0)
+    rng.shuffle(cand)
+    # calibrate: ~2 GFLOP/s per core for a first guess, then grow
+    budget = seconds * threads * 8e9
+    sel, acc = [], 0.0
+    for t in cand:
+        sel.append(t)
+        acc += tile_fl[t]
+        if acc >= budget:
+            break
+    sel = np.asarray(sorted(sel), np.int64)
+    msz = nsz = ksz = sizes.astype(np.int64)
+    res_off = np.full(nt * nt, -1, np.int64)
+    pos = 0
+    for t in sel:
+        res_off[t] = pos
+        pos += int(sizes[t // nt] * sizes[t % nt])
+    cbuf = np.zeros(max(pos, 1))
+    L = O.lib()
+    P = lambda a, ty: a.ctypes.data_as(ty)
+    t0 = time.perf_counter()
+    L.orc_contract_subset(nt, nt, nt, P(msz, O._i64p), P(nsz, O._i64p), P(ksz, O._i64p),
+                          P(A_t["data"], O._f64p), P(A_t["offsets"], O._i64p), 0,
+                          P(B_t["data"], O._f64p), P(B_t["offsets"], O._i64p), 0,
+                          P(offs, O._i64p), P(kidx, O._i32p), 1.0, P(cbuf, O._f64p),
+                          P(res_off, O._i64p), P(sel, O._i64p), len(sel), threads, fn)
+    dt = time.perf_counter() - t0
+    fl = tile_fl[sel].sum()
+    desc = (f"{len(sel)} of {len(cand)} nonzero result tiles ({fl / tile_fl.sum() * 100:.2f}% "
+            f"of the flops), per-pair {'OpenBLAS' if fn else 'oracle-loop'} dgemm, {threads} threads")
+    return fl / dt / 1e12, desc, dt
+
+
+def run_reference(args):
+    """CPU reference arm: the oracle port (the reference cannot be built here),
+    all host threads, bounded samples of the same workload."""
+    ws, rank, local = dist_env()
+    if ws > 1 and rank != 0:
+        return
+    import oracle as O
+    from oracle import build as ob
+    ob.build()
+    h, scale = workload(args.n, args.seed)
+    nt = len(h) - 1
+    thr = 1e-8
+    t0 = time.perf_counter()
+    tr = O.TiledRange([h, h])
+    A = O.make_array(tr, args.seed, 0, 0, tile_scale=lambda i: float(scale[i[0], i[1]]),
+                     keep=lambda i: scale[i[0], i[1]] != 0, threshold=thr)
+    B = O.make_array(tr, args.seed, 1, 0, tile_scale=lambda i: float(scale[i[0], i[1]]),
+                     keep=lambda i: scale[i[0], i[1]] != 0, threshold=thr)
+
+    def pack(X):
+        offs = np.full(nt * nt, -1, np.int64)
+        bufs, pos = [], 0
+        for o in range(nt * nt):
+            t = X.tiles.get(o)
+            if t is not None:
+                offs[o] = pos
+                bufs.append(t.ravel())
+                pos += t.size
+        return {"data": np.concatenate(bufs), "offsets": offs, "norms": X.norms.ravel()}
+    At, Bt = pack(A), pack(B)
+    threads = os.cpu_count() or 1
+    vals, desc = [], ""
+    per_step = max(2.0, min(20.0, 120.0 / max(1, args.steps + args.warmup)))
+    for s in range(args.warmup + args.steps):
+        v, desc, dt = cpu_sample(At, Bt, h, scale, per_step, threads, seed=s)
+        if s >= args.warmup:
+            vals.append((v, dt))
+    v = statistics.median(x[0] for x in vals)
+    ms = statistics.median(x[1] for x in vals) * 1e3
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded, generated on the host)",
+            "config": {"workload": f"block-sparse matmul TSpArrayD N={args.n}, tiles U[48,256], "
+                                   "exp(-|I-J|/4) blocks, threshold 1e-8",
+                       "sample": desc},
+            "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "setup_s": time.perf_counter() - t0}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="tagpu", choices=["tagpu", "reference"])
+    ap.add_argument("--precision", default="ozaki", choices=["ozaki", "fp64"])
+    ap.add_argument("--slices", type=int, default=6)
+    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+
+    import tiledarray_gb300 as ta
+    from tiledarray_gb300 import build as tb
+    tb.build()
+    w = ta.World(local)
+    thr = 1e-8
+    w.threshold = thr
+    h, scale = workload(args.n, args.seed)
+    nt = len(h) - 1
+    tr = ta.TiledRange([h, h])
+    A = ta.DistArray(w, tr)
+    B = ta.DistArray(w, tr)
+    A.generate(args.seed, 0, 0, scale, True, thr)
+    B.generate(args.seed, 1, 0, scale, True, thr)
+    prec = ta.PRECISION_OZAKI if args.precision == "ozaki" else ta.PRECISION_FP64
+
+    def step():
+        C, st = ta.contract(w, "i,j", 1.0, A, "i,k", B, "k,j", precision=prec,
+                            slices=args.slices)
+        return C, st
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        C, st = step()
+        del C
+    barrier()
+    w.sync()
+    clk = Clocks(local)
+    ms_list, stats = [], None
+    for _ in range(args.steps):
+        w.timer_start()
+        C, stats = step()
+        ms_list.append(w.timer_stop())
+        if _ != args.steps - 1:
+            del C
+    w.sync()
+    barrier()
+    clocks = clk.stop()
+    total_ms = sum(ms_list)
+    if dist is not None:
+        import torch
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    flops = stats["flops"]
+    ms_step = total_ms / args.steps
+    value = flops * ws / (ms_step * 1e-3) / 1e12
+    lat = sorted(ms_list)
+    p50 = float(np.percentile(lat, 50))
+    p99 = float(np.percentile(lat, 99))
+    hbm_peak, bf16_peak, peak_kind = peaks()
+    pairs_per = SLICE_PAIRS.get(args.slices, 21) if prec == ta.PRECISION_OZAKI else 1
+    gemm_ms = stats["ms_gemm"]
+    if prec == ta.PRECISION_OZAKI:
+        achieved = flops * pairs_per / (gemm_ms * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": achieved / bf16_peak, "traffic": None,
+                "kernel": "ozaki_gemm (bf16 digit-slice products, "
+                          f"{pairs_per} per FP64 product)", "peak_kind": f"{peak_kind} bf16 burst"}
+    else:
+        achieved = flops / (gemm_ms * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
+                "frac": achieved / 1.25, "traffic": None, "kernel": "dmma_gemm",
+                "peak_kind": "nominal FP64 (no measured FP64 peak)"}
+    out = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64 (emulated: bf16 digit slices, exact int accumulation)"
+           if prec == ta.PRECISION_OZAKI else "f64",
+           "data": "synthetic (seeded counter-based generator, on device)",
+           "config": {"workload": f"block-sparse matmul TSpArrayD N={args.n}, tiles U[48,256] "
+                                  f"({nt} per dim), exp(-|I-J|/4) blocks cut at 1e-10, "
+                                  "threshold 1e-8",
+                      "precision": args.precision, "slices": args.slices if
+                      prec == ta.PRECISION_OZAKI else None,
+                      "pairs": stats["pairs"], "flops_per_step": flops,
+                      "nonzero_result_tiles": stats["nonzero_result_tiles"],
+                      "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"},
+           "latency_ms": {"p50": p50, "p99": p99},
+           "phases_ms": {k: stats[k] for k in ("ms_shape", "ms_pairs", "ms_split", "ms_gemm")},
+           "roofline": roof, "clocks": clocks,
+           "gpu_launches": int(4 + stats["gemm_launches"])}
+    # error vs plain FP64 (DMMA) on the device, and the plain form's speed
+    if rank == 0 and not args.no_plain and prec == ta.PRECISION_OZAKI:
+        Cp, stp = ta.contract(w, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_FP64)
+        x, y = C.download(), Cp.download()
+        err = float(np.linalg.norm(x - y) / np.linalg.norm(y))
+        out["plain_fp64"] = {"value": flops / (stp["ms_total"] * 1e-3) / 1e12,
+                             "ms_per_step": stp["ms_total"], "ms_gemm": stp["ms_gemm"],
+                             "unit": "TFLOP/s"}
+        out["rel_err_vs_plain_fp64"] = err
+        out["emulated_over_plain"] = value / out["plain_fp64"]["value"]
+        del Cp, x, y
+    # end to end through the public API with host buffers
+    if rank == 0 and not args.no_e2e:
+        import torch
+        a_host = torch.empty(A.info().elements, dtype=torch.float64, pin_memory=True).numpy()
+        b_host = torch.empty(B.info().elements, dtype=torch.float64, pin_memory=True).numpy()
+        a_host[:] = A.download()
+        b_host[:] = B.download()
+        c_host = None
+        e2e_ms = []
+        for _ in range(max(1, min(args.steps, 3))):
+            t0 = time.perf_counter()
+            A.upload(a_host)
+            B.upload(b_host)
+            C2, st2 = step()
+            n = C2.info().elements
+            if c_host is None:
+                c_host = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+            w.check(w.L.tagpu_array_download(C2.h, c_host.ctypes.data_as(ta._f64p), n))
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+            del C2
+        e = statistics.median(e2e_ms)
+        out["e2e"] = {"value": flops / (e * 1e-3) / 1e12, "unit": "TFLOP/s",
+                      "h2d_bytes_per_step": int(a_host.nbytes + b_host.nbytes),
+                      "d2h_bytes_per_step": int(c_host.nbytes), "ms_per_step": e}
+        if not args.no_cpu:
+            A_t = {"data": a_host, "offsets": A.tile_offsets(), "norms": A.norms()}
+            B_t = {"data": b_host, "offsets": B.tile_offsets(), "norms": B.norms()}
+            threads = os.cpu_count() or 1
+            v, desc, dt = cpu_sample(A_t, B_t, h, scale, args.cpu_seconds, threads)
+            out["cpu_baseline"] = {"value": v, "unit": "TFLOP/s", "cores": threads,
+                                   "kind": "port", "sample": desc, "seconds": dt}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    del A, B, C
+    w.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

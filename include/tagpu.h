@@ -84,6 +84,11 @@ const char* tagpu_status_string(tagpu_status s);
 /* Blocks until all work queued on the context has finished. */
 tagpu_status tagpu_sync(tagpu_ctx* ctx);
 
+/* CUDA-event timing on the context's stream: start records an event, stop
+ * records a second one, waits for it and returns the elapsed milliseconds. */
+tagpu_status tagpu_timer_start(tagpu_ctx* ctx);
+tagpu_status tagpu_timer_stop(tagpu_ctx* ctx, double* ms);
+
 /* Default screening threshold used for new result shapes; initial value is
  * FLT_EPSILON as in SparseShape<float>. */
 float tagpu_threshold_get(const tagpu_ctx* ctx);

@@ -1,0 +1,31 @@
+"""The C++ façade (include/tagpu/tiledarray.hpp) compiles TiledArray-style
+expressions unchanged and runs them through libtagpu.so."""
+import os
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def build_facade(tmp_path):
+    from tiledarray_gb300 import build as tb
+    lib = tb.build()
+    exe = str(tmp_path / "test_facade")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "test_facade.cpp"), "-o", exe,
+                    lib, "-Wl,-rpath," + os.path.dirname(lib)], check=True)
+    return exe
+
+
+def test_facade_compiles(tmp_path):
+    assert os.path.exists(build_facade(tmp_path))
+
+
+@pytest.mark.gpu
+def test_facade_runs(tmp_path):
+    exe = build_facade(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    print(r.stdout, r.stderr)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.count("ok ") == 3

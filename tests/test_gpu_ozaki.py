@@ -1,0 +1,139 @@
+"""GPU parity of the emulated-FP64 form (bf16 digit slices on tcgen05).
+
+Integer-valued data are represented exactly by the digits and every level
+sum is exact integer arithmetic, so those results must equal the golden
+values bit for bit; uniform[-1,1) data must stay within 1e-12 relative
+Frobenius error of the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from helpers import contraction_cases, golden, gpu_operand, oracle_operand, rel_fro
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def ta():
+    import tiledarray_gb300 as ta
+    return ta
+
+
+def uneven(n, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    h = [0]
+    while h[-1] < n:
+        h.append(min(n, h[-1] + int(rng.integers(lo, hi + 1))))
+    return h
+
+
+@pytest.mark.parametrize("case", contraction_cases(), ids=lambda c: c["tag"])
+def test_ozaki_golden_exact(ta, world, case):
+    A, _ = gpu_operand(ta, world, case["trange_a"], *case["seed_a"], kind=1, keep=case["keep_a"])
+    B, _ = gpu_operand(ta, world, case["trange_b"], *case["seed_b"], kind=1, keep=case["keep_b"])
+    C, st = ta.contract(world, case["c"], case["alpha"], A, case["a"], B, case["b"],
+                        precision=ta.PRECISION_OZAKI)
+    exp = golden(f"contract_{case['tag']}.npz")["expected"]
+    assert np.array_equal(C.to_dense(C.trange), exp)
+
+
+@pytest.mark.parametrize("n,lo,hi,seed,decay", [(600, 48, 256, 1, 2.0), (1500, 48, 256, 2, 4.0),
+                                                (700, 1, 90, 3, 3.0), (2100, 200, 256, 4, 8.0)])
+def test_ozaki_uniform_vs_oracle(oracle, ta, world, n, lo, hi, seed, decay):
+    h = uneven(n, lo, hi, seed)
+    nt = len(h) - 1
+    I, J = np.meshgrid(np.arange(nt), np.arange(nt), indexing="ij")
+    scale = np.exp(-np.abs(I - J) / decay)
+    scale[scale < 1e-10] = 0
+    thr = 1e-8
+    A, _ = gpu_operand(ta, world, [h, h], seed, 0, kind=0, tile_scale=scale, threshold=thr)
+    B, _ = gpu_operand(ta, world, [h, h], seed, 1, kind=0, tile_scale=scale, threshold=thr)
+    world.threshold = thr
+    try:
+        C, st = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI)
+        Cp, stp = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j")
+    finally:
+        world.threshold = ta.FLT_EPSILON
+    Ao = oracle_operand(oracle, [h, h], seed, 0, kind=0, tile_scale=scale, threshold=thr)
+    Bo = oracle_operand(oracle, [h, h], seed, 1, kind=0, tile_scale=scale, threshold=thr)
+    ref = oracle.contract("i,j", Ao, "i,k", Bo, "k,j", threshold=thr).to_dense()
+    got = C.to_dense(C.trange)
+    err = rel_fro(got, ref)
+    print(f"ozaki rel err {err:.3e}, plain {rel_fro(Cp.to_dense(Cp.trange), ref):.3e}")
+    assert err <= TOL
+    assert np.array_equal(C.norms(), Cp.norms())
+    assert st["pairs"] == stp["pairs"]
+
+
+@pytest.mark.parametrize("slices,bound", [(4, 1e-7), (5, 1e-9), (6, 1e-12), (7, 1e-12)])
+def test_ozaki_slices(oracle, ta, world, slices, bound):
+    h = uneven(400, 40, 120, 9)
+    A, _ = gpu_operand(ta, world, [h, h], 5, 0, kind=0)
+    B, _ = gpu_operand(ta, world, [h, h], 5, 1, kind=0)
+    C, st = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI,
+                        slices=slices)
+    Ao = oracle_operand(oracle, [h, h], 5, 0, kind=0)
+    Bo = oracle_operand(oracle, [h, h], 5, 1, kind=0)
+    ref = oracle.contract("i,j", Ao, "i,k", Bo, "k,j").to_dense()
+    err = rel_fro(C.to_dense(C.trange), ref)
+    print(f"slices={slices} rel err {err:.3e}")
+    assert err <= bound
+
+
+def test_ozaki_carry_normalisation_exact(ta, world):
+    """All-positive integer data over a long k: every level grows at the
+    worst-case rate, so the carries must keep the fp32 sums exact."""
+    hk = uneven(6000, 100, 256, 11)
+    hm = [0, 130, 257]
+    A, _ = gpu_operand(ta, world, [hm, hk], 1, 0, kind=1)
+    B, _ = gpu_operand(ta, world, [hk, hm], 1, 1, kind=1)
+    C, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI)
+    Cp, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j")
+    assert np.array_equal(C.download(), Cp.download())
+
+
+def test_ozaki_transposed_and_4index(oracle, ta, world):
+    h1, h2 = [0, 40, 96], [0, 32, 70, 96]
+    for c, a, b, tra, trb in [("i,j", "k,i", "j,k", [h2, h1], [h1, h2]),
+                              ("a,b,i,j", "a,b,c,d", "c,d,i,j", [h1, h2, h1, h2],
+                               [h1, h2, h1, h2]),
+                              ("i,j,a,b", "a,c,b,d", "c,d,i,j", [h1, h1, h2, h2],
+                               [h1, h2, h1, h2])]:
+        A, _ = gpu_operand(ta, world, tra, 2, 0, kind=0)
+        B, _ = gpu_operand(ta, world, trb, 2, 1, kind=0)
+        C, _ = ta.contract(world, c, 0.5, A, a, B, b, precision=ta.PRECISION_OZAKI)
+        Ao = oracle_operand(oracle, tra, 2, 0, kind=0)
+        Bo = oracle_operand(oracle, trb, 2, 1, kind=0)
+        ref = oracle.contract(c, Ao, a, Bo, b, 0.5).to_dense()
+        assert rel_fro(C.to_dense(C.trange), ref) <= TOL
+
+
+def test_ozaki_batch_graph(ta, world):
+    import ctypes
+    L = world.L
+    h = uneven(500, 48, 200, 13)
+    pairs = []
+    for x in range(3):
+        A, _ = gpu_operand(ta, world, [h, h], 7, 2 * x, kind=0)
+        B, _ = gpu_operand(ta, world, [h, h], 7, 2 * x + 1, kind=0)
+        pairs.append((A, B))
+    bh = ctypes.c_void_p()
+    world.check(L.tagpu_batch_create(world.h, ctypes.byref(bh)))
+    outs = []
+    for A, B in pairs:
+        ch = ctypes.c_void_p()
+        opts = ta.ContractOpts(ta.PRECISION_OZAKI, 6, -1.0)
+        world.check(L.tagpu_batch_add(bh, b"i,j", 1.0, A.h, b"i,k", B.h, b"k,j",
+                                      ctypes.byref(opts), ctypes.byref(ch)))
+        outs.append(ta.DistArray(world, _handle=ch))
+    world.check(L.tagpu_batch_run(bh))
+    first = [o.download().copy() for o in outs]
+    for (A, B), f in zip(pairs, first):
+        ref, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI)
+        assert np.array_equal(ref.download(), f)
+    world.check(L.tagpu_batch_run(bh))
+    for o, f in zip(outs, first):
+        assert np.array_equal(o.download(), f)
+    world.check(L.tagpu_batch_destroy(bh))

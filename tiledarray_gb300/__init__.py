@@ -86,6 +86,8 @@ SIGNATURES = {
     "tagpu_last_error": (ctypes.c_char_p, [_vp]),
     "tagpu_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "tagpu_sync": (ctypes.c_int, [_vp]),
+    "tagpu_timer_start": (ctypes.c_int, [_vp]),
+    "tagpu_timer_stop": (ctypes.c_int, [_vp, _f64p]),
     "tagpu_threshold_get": (ctypes.c_float, [_vp]),
     "tagpu_threshold_set": (None, [_vp, ctypes.c_float]),
     "tagpu_array_create": (ctypes.c_int, [_vp, ctypes.c_int, _i64p,
@@ -170,6 +172,14 @@ class World:
 
     def sync(self):
         self.check(self.L.tagpu_sync(self.h))
+
+    def timer_start(self):
+        self.check(self.L.tagpu_timer_start(self.h))
+
+    def timer_stop(self):
+        ms = ctypes.c_double(0)
+        self.check(self.L.tagpu_timer_stop(self.h, ctypes.byref(ms)))
+        return ms.value
 
     def last_stats(self):
         s = ContractStats()

@@ -93,9 +93,19 @@ void launch_dmma_gemm(cudaStream_t s, const GemmView* views, const WorkItem* ite
                       int64_t nitems, int sm_count);
 
 // (d) emulated FP64 (Ozaki scheme, bf16 digit slices on tcgen05).
+// ozaki_plan sizes and fills the scratch (index maps, brick maps, block
+// lists; host synchronises to read counts); ozaki_enqueue runs the frames and
+// the digit splitting, ozaki_enqueue_gemm the tensor-core GEMM; neither
+// synchronises, so both can be captured in a CUDA graph.
 struct OzakiPlan;
-tagpu_status ozaki_run(cudaStream_t s, const GemmView& v, int slices,
-                       int sm_count, size_t* scratch_bytes, double* ms_split,
-                       double* ms_gemm, int64_t* blocks, std::string* err);
+tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
+                        const int32_t* h_nsz, const int32_t* h_ksz, int slices,
+                        OzakiPlan** out, std::string* err);
+void ozaki_enqueue(OzakiPlan* pl, int sm_count);
+void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count);
+int ozaki_error(OzakiPlan* pl);   // synchronises; 0 = ok
+size_t ozaki_scratch_bytes(const OzakiPlan* pl);
+int64_t ozaki_blocks(const OzakiPlan* pl);
+void ozaki_destroy(OzakiPlan* pl);
 
 }  // namespace tagpu

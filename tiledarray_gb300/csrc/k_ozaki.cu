@@ -1,14 +1,1025 @@
-// Kernel (d), emulated FP64 form (Ozaki scheme on the tcgen05 tensor cores).
+// Kernel (d), emulated-FP64 form: Ozaki-style split-integer slices on the
+// tcgen05 tensor cores of sm_103a.
+//
+// What is computed: the same per-result-tile reduction as the plain DMMA
+// kernel, C(i,j) = alpha * sum_k A(i,k) B(k,j) over the tile-pair list, with
+// an error against FP64 of order 2^-48 relative per product.
+//
+// How:
+//  * frames: every fused row r of A gets E_A[r] with |A[r,:]| < 2^E_A[r], every
+//    fused column c of B gets E_B[c] (one pass over the operands, integer ops
+//    on the IEEE bit fields);
+//  * splitting (integer only): a = x * 2^-E rounded to 8S-1 fractional bits is
+//    cut into S balanced base-256 digits d_1..d_S, |d_p| <= 128, so that
+//    a = sum_p d_p 2^(1-8p).  Digits are exact in bf16.  They are written into
+//    "bricks" (128 rows x 32 k for A, 64 columns x 32 k for B, in global fused
+//    coordinates) laid out exactly as the K-major no-swizzle UMMA operand image
+//    in shared memory, so one bulk copy moves a brick into place;
+//  * products: for each pair (p, q) with p + q <= S + 1 one
+//    tcgen05.mma.kind::f16 (bf16 x bf16 -> fp32, M=128, N=64, K=16) adds
+//    D_p * E_q into the accumulator of level t = p + q in tensor memory.  All
+//    products are integers below 2^14 and every level is kept below 2^24 by
+//    a carry normalisation every 128 k (digits above 2^8 move one level up, the
+//    top level L1 only collects carries), so every fp32 sum is exact integer
+//    arithmetic;
+//  * recombination (the only FP64 arithmetic): at the end of an
+//    output block, C = alpha * 2^(E_A + E_B) * sum_t L_t 2^(2-8t), written into
+//    the result tiles the block overlaps.
+// Work is in global fused coordinates (output blocks 128 x 64, k blocks of
+// 32), so uneven tiles cost no padding except at block-sparsity boundaries;
+// a brick is stored only if some nonzero tile overlaps it, a k block is run
+// for an output block only if both bricks exist.  Contributions of absent
+// pairs are exact zeros, and output elements of zero result tiles are never
+// written, so the result equals the tile-pair-list reduction.
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <memory>
+#include <string>
+#include <vector>
 
 #include "internal.h"
 
 namespace tagpu {
+namespace {
 
-tagpu_status ozaki_run(cudaStream_t, const GemmView&, int, int, size_t*, double*, double*,
-                       int64_t*, std::string* err) {
-  *err = "emulated FP64 form not built yet";
-  return TAGPU_ERR_UNSUPPORTED;
+constexpr int BM = 128;            // output block rows (MMA M)
+constexpr int BN = 64;             // output block columns (MMA N)
+constexpr int BK = 32;             // k per stage (two MMA K = 16 steps)
+constexpr int NORM_STAGES = 4;     // carry normalisation every 128 k
+constexpr int A_SLICE_BYTES = BM * BK * 2;   // 8 KB
+constexpr int B_SLICE_BYTES = BN * BK * 2;   // 4 KB
+constexpr int EPI_WARPS = 4;
+constexpr int THREADS = 64 + EPI_WARPS * 32; // producer, MMA, 4 epilogue warps
+constexpr unsigned long long WAIT_NS = 4000000000ull;  // 4 s bound per wait
+
+// ---------------------------------------------------------------------------
+// PTX wrappers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
 }
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false after WAIT_NS or when another role has aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile int* abort_s) {
+  if (mbar_try(a, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  for (uint32_t i = 0;; ++i) {
+    if (mbar_try(a, parity)) return true;
+    if ((i & 63) == 63) {
+      if (*abort_s) return false;
+      if (globaltimer() - t0 > WAIT_NS) return false;
+    }
+  }
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(dst), "l"(src), "r"(bytes), "r"(mbar)
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+               ::"r"(mbar)
+               : "memory");
+}
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                       uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+      ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+      "%13,%14,%15,%16};"
+      ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])),
+        "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])),
+        "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+        "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])),
+        "r"(__float_as_uint(v[11])), "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])),
+        "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+// K-major, no-swizzle operand image: core matrices of 8 rows x 16 bytes,
+// LBO = 128 B between the K-adjacent core matrices, SBO = 512 B between
+// 8-row groups (a 32-k brick row group holds 4 core matrices).
+__host__ __device__ inline uint32_t brick_offset(int row, int k) {
+  return (uint32_t)((row >> 3) * 512 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)(128 >> 4) << 16;   // leading byte offset (K direction)
+  d |= (uint64_t)(512 >> 4) << 32;   // stride byte offset (M/N direction)
+  d |= (uint64_t)1 << 46;            // descriptor version for tcgen05
+  return d;                          // base offset 0, layout SWIZZLE_NONE
+}
+// kind::f16 instruction descriptor: D f32, A/B bf16, K-major, N=64, M=128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                            ((uint32_t)(BM >> 4) << 24);
+
+// 2^(2 - 8t): the unit of level t (products of digits d_p e_q with p + q = t)
+__device__ __forceinline__ double level_unit(int t) {
+  return __longlong_as_double((long long)(1023 + 2 - 8 * t) << 52);
+}
+
+struct OzParams {
+  const uint8_t* Apack;      // A bricks, S * 8 KB each
+  const uint8_t* Bpack;      // B bricks, S * 4 KB each
+  const int32_t* brickA;     // RB x KBn -> slot or -1
+  const int32_t* brickB;     // KBn x CB -> slot or -1
+  const int32_t* blk;        // nblk x 2 (rb, cb)
+  const int64_t* blk_off;    // nblk + 1
+  const int32_t* blk_kb;     // k blocks per output block
+  int64_t nblk;
+  int KBn, CB;
+  const int32_t* EA;         // M_total frames (biased exponent; E = EA - 1022)
+  const int32_t* EB;         // N_total frames
+  const int32_t* row_tile;   // M_total
+  const int32_t* row_local;
+  const int32_t* col_tile;   // N_total
+  const int32_t* col_local;
+  const int32_t* nsz;
+  int64_t Nt;
+  const int64_t* coff;       // Mt*Nt result tile offsets
+  double alpha;
+  double* C;
+  int64_t M_total, N_total;
+  int* err;                  // error flag (0 = ok)
+};
+
+template <int S>
+struct Smem {
+  static constexpr int kStages = (S * (A_SLICE_BYTES + B_SLICE_BYTES) * 3 <= 200 * 1024) ? 3 : 2;
+  static constexpr int kStageBytes = S * (A_SLICE_BYTES + B_SLICE_BYTES);
+  static constexpr int kBytes = kStages * kStageBytes + 1024;
+};
+
+template <int S>
+__global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(OzParams P) {
+  constexpr int STAGES = Smem<S>::kStages;
+  constexpr int STAGE_BYTES = Smem<S>::kStageBytes;
+  constexpr int LEVELS = S + 1;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES];
+  __shared__ __align__(8) uint64_t bar_acc_full, bar_acc_empty, bar_done;
+  __shared__ uint32_t tmem_base_s;
+  __shared__ volatile int abort_s;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint8_t* stage_base = (uint8_t*)(((uintptr_t)smem + 1023) & ~(uintptr_t)1023);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(smem_u32(&bar_full[s]), 1);
+      mbar_init(smem_u32(&bar_empty[s]), 1);
+    }
+    mbar_init(smem_u32(&bar_acc_full), 1);
+    mbar_init(smem_u32(&bar_acc_empty), EPI_WARPS * 32);
+    mbar_init(smem_u32(&bar_done), 1);
+    abort_s = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;"
+                 ::"r"(smem_u32(&tmem_base_s)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_s;
+
+  auto fail = [&](int code) {
+    abort_s = 1;
+    atomicCAS(P.err, 0, code);
+  };
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      uint32_t issued_parity[STAGES];
+      bool issued[STAGES];
+      for (int s = 0; s < STAGES; ++s) issued[s] = false;
+      bool ok = true;
+      for (int64_t b = blockIdx.x; b < P.nblk && ok; b += gridDim.x) {
+        const int rb = P.blk[2 * b], cb = P.blk[2 * b + 1];
+        for (int64_t x = P.blk_off[b]; x < P.blk_off[b + 1]; ++x) {
+          const int kb = P.blk_kb[x];
+          if (!mbar_wait(smem_u32(&bar_empty[stage]), phase ^ 1, &abort_s)) {
+            fail(1);
+            ok = false;
+            break;
+          }
+          const int sa = P.brickA[(int64_t)rb * P.KBn + kb];
+          const int sb = P.brickB[(int64_t)kb * P.CB + cb];
+          uint8_t* dst = stage_base + stage * STAGE_BYTES;
+          const uint32_t full = smem_u32(&bar_full[stage]);
+          mbar_expect_tx(full, STAGE_BYTES);
+          bulk_g2s(smem_u32(dst), P.Apack + (size_t)sa * (S * A_SLICE_BYTES), S * A_SLICE_BYTES,
+                   full);
+          bulk_g2s(smem_u32(dst + S * A_SLICE_BYTES), P.Bpack + (size_t)sb * (S * B_SLICE_BYTES),
+                   S * B_SLICE_BYTES, full);
+          issued[stage] = true;
+          issued_parity[stage] = phase;
+          if (++stage == STAGES) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      // copies still in flight land before the CTA may exit
+      for (int s = 0; s < STAGES; ++s)
+        if (issued[s] && !mbar_wait(smem_u32(&bar_full[s]), issued_parity[s], &abort_s)) {
+          // the abort flag may be set: wait once more without it
+          const uint64_t t0 = globaltimer();
+          while (!mbar_try(smem_u32(&bar_full[s]), issued_parity[s]) &&
+                 globaltimer() - t0 < WAIT_NS) {
+          }
+        }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    int stage = 0;
+    uint32_t phase = 0, acc_phase = 0;
+    bool ok = true;
+    for (int64_t b = blockIdx.x; b < P.nblk && ok; b += gridDim.x) {
+      const int64_t n = P.blk_off[b + 1] - P.blk_off[b];
+      for (int64_t x = 0; x < n && ok; ++x) {
+        if (!mbar_wait(smem_u32(&bar_full[stage]), phase, &abort_s)) {
+          fail(2);
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        if (lane == 0) {
+          const uint32_t sbase = smem_u32(stage_base + stage * STAGE_BYTES);
+          const bool fresh = (x == 0);
+#pragma unroll
+          for (int ks = 0; ks < 2; ++ks) {
+#pragma unroll
+            for (int t = 2; t <= S + 1; ++t) {
+#pragma unroll
+              for (int p = 1; p < t; ++p) {
+                const int q = t - p;
+                if (p > S || q > S) continue;
+                const uint32_t a = sbase + (p - 1) * A_SLICE_BYTES + ks * 256;
+                const uint32_t bb = sbase + S * A_SLICE_BYTES + (q - 1) * B_SLICE_BYTES + ks * 256;
+                const uint32_t acc = (fresh && ks == 0 && p == 1) ? 0u : 1u;
+                tc_mma(tmem + (t - 1) * BN, make_desc(a), make_desc(bb), kIdesc, acc);
+              }
+            }
+          }
+          tc_commit(smem_u32(&bar_empty[stage]));
+        }
+        __syncwarp();
+        if (++stage == STAGES) {
+          stage = 0;
+          phase ^= 1;
+        }
+        const bool last = (x == n - 1);
+        if (last || ((x + 1) % NORM_STAGES) == 0) {
+          if (lane == 0) tc_commit(smem_u32(&bar_acc_full));
+          __syncwarp();
+          if (!mbar_wait(smem_u32(&bar_acc_empty), acc_phase, &abort_s)) {
+            fail(3);
+            ok = false;
+            break;
+          }
+          acc_phase ^= 1;
+          tc_fence_after();
+        }
+      }
+    }
+    // nothing may be in flight when tensor memory is released
+    if (lane == 0) tc_commit(smem_u32(&bar_done));
+    __syncwarp();
+    {
+      const uint64_t t0 = globaltimer();
+      while (!mbar_try(smem_u32(&bar_done), 0) && globaltimer() - t0 < WAIT_NS) {
+      }
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int quarter = warp & 3;
+    const int rloc = quarter * 32 + lane;
+    const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
+    uint32_t acc_phase = 0;
+    {
+      // L1 only collects carries: start from zero
+      float z[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) z[i] = 0.0f;
+#pragma unroll
+      for (int c = 0; c < BN; c += 16) tmem_st16(lane_addr + c, z);
+      tmem_wait_st();
+    }
+    bool ok = true;
+    for (int64_t b = blockIdx.x; b < P.nblk && ok; b += gridDim.x) {
+      const int rb = P.blk[2 * b], cb = P.blk[2 * b + 1];
+      const int64_t n = P.blk_off[b + 1] - P.blk_off[b];
+      const int64_t events = (n + NORM_STAGES - 1) / NORM_STAGES;
+      for (int64_t ev = 0; ev < events; ++ev) {
+        if (!mbar_wait(smem_u32(&bar_acc_full), acc_phase, &abort_s)) {
+          fail(4);
+          ok = false;
+          break;
+        }
+        acc_phase ^= 1;
+        tc_fence_after();
+        const bool final_ev = (ev == events - 1);
+        if (!final_ev) {
+          // carry normalisation: every level back to |L_t| <= 128 (t >= 2)
+#pragma unroll 1
+          for (int c = 0; c < BN; c += 16) {
+            float L[LEVELS][16];
+#pragma unroll
+            for (int t = 0; t < LEVELS; ++t) tmem_ld16(lane_addr + t * BN + c, L[t]);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              float carry = 0.0f;
+#pragma unroll
+              for (int t = LEVELS - 1; t >= 1; --t) {
+                const float xv = L[t][j] + carry;
+                const float h = rintf(xv * 0.00390625f);
+                L[t][j] = fmaf(-256.0f, h, xv);
+                carry = h;
+              }
+              L[0][j] += carry;
+            }
+#pragma unroll
+            for (int t = 0; t < LEVELS; ++t) tmem_st16(lane_addr + t * BN + c, L[t]);
+            tmem_wait_st();
+          }
+        } else {
+          // recombination and store into the result tiles
+          const int64_t gr = (int64_t)rb * BM + rloc;
+          const bool row_ok = gr < P.M_total;
+          int ti = 0, lr = 0, ea = 0;
+          if (row_ok) {
+            ti = P.row_tile[gr];
+            lr = P.row_local[gr];
+            ea = P.EA[gr];
+          }
+#pragma unroll 1
+          for (int c = 0; c < BN; c += 16) {
+            float L[LEVELS][16];
+#pragma unroll
+            for (int t = 0; t < LEVELS; ++t) tmem_ld16(lane_addr + t * BN + c, L[t]);
+            tmem_wait_ld();
+            if (row_ok) {
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                const int64_t gc = (int64_t)cb * BN + c + j;
+                if (gc < P.N_total) {
+                  const int tj = P.col_tile[gc];
+                  const int64_t off = P.coff[(int64_t)ti * P.Nt + tj];
+                  if (off >= 0) {
+                    double v = 0.0;
+#pragma unroll
+                    for (int t = LEVELS - 1; t >= 0; --t)
+                      v = fma((double)L[t][j], level_unit(t + 1), v);
+                    const double val = P.alpha * ldexp(v, (ea - 1022) + (P.EB[gc] - 1022));
+                    P.C[off + (int64_t)lr * P.nsz[tj] + P.col_local[gc]] = val;
+                  }
+                }
+              }
+            }
+          }
+          // zero L1 for the next block
+          float z[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) z[i] = 0.0f;
+#pragma unroll
+          for (int c = 0; c < BN; c += 16) tmem_st16(lane_addr + c, z);
+          tmem_wait_st();
+        }
+        tc_fence_before();
+        mbar_arrive(smem_u32(&bar_acc_empty));
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// frames, bricks and splitting
+// ---------------------------------------------------------------------------
+
+// Element (row, k) of an operand in GEMM order.  A: rows = M, tile (i,k) is
+// m x kk (trans: kk x m).  B is seen as its transpose: rows = N, tile (k,j)
+// is kk x n (trans: n x kk).
+struct OperandView {
+  const double* data;
+  const int64_t* off;        // tile offsets
+  int64_t rowt, kt;          // tile grid (rows, k) in this view
+  int64_t off_stride_row, off_stride_k;  // off index = rt*sr + kt*sk
+  const int32_t* rsz;        // tile sizes along rows
+  const int32_t* ksz;        // tile sizes along k
+  int row_contig;            // 1: element (r, k) at r * 1 + k * rows_in_tile
+};
+
+__device__ __forceinline__ int exp_field(double x) {
+  return (int)((__double_as_longlong(x) >> 52) & 0x7ff);
+}
+
+// One warp per (tile, local row): max biased exponent over the row's k.
+__global__ void frame_kernel(OperandView v, const int32_t* __restrict__ row_start,
+                             const int64_t* __restrict__ work, int64_t nwork,
+                             int32_t* __restrict__ E) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= nwork) return;
+  // work: tile ordinal (rt*kt_count + kt) << 20 | local row
+  const int64_t packed = work[w];
+  const int64_t t = packed >> 20;
+  const int lr = (int)(packed & 0xfffff);
+  const int64_t rt = t / v.kt, ktile = t - (t / v.kt) * v.kt;
+  const int64_t o = v.off[rt * v.off_stride_row + ktile * v.off_stride_k];
+  if (o < 0) return;
+  const int m = v.rsz[rt], kk = v.ksz[ktile];
+  const double* base = v.data + o;
+  int e = 0;
+  for (int k = lane; k < kk; k += 32) {
+    const double x = v.row_contig ? base[(int64_t)k * m + lr] : base[(int64_t)lr * kk + k];
+    e = max(e, exp_field(x));
+  }
+  for (int s = 16; s > 0; s >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, s));
+  if (lane == 0 && e > 0) atomicMax(&E[row_start[rt] + lr], e);
+}
+
+// One CTA per brick: gather ROWS x 32 elements, split into S digit slices,
+// write the brick image.
+template <int S, int ROWS>
+__global__ void __launch_bounds__(256) split_kernel(
+    OperandView v, const int32_t* __restrict__ row_tile, const int32_t* __restrict__ row_local,
+    const int32_t* __restrict__ k_tile, const int32_t* __restrict__ k_local,
+    const int32_t* __restrict__ E, int64_t rows_total, int64_t k_total,
+    const int32_t* __restrict__ bricks /* nbricks x 2 (rowblock, kblock) */, int64_t nbricks,
+    uint8_t* __restrict__ pack) {
+  constexpr int SLICE = ROWS * BK * 2;
+  extern __shared__ __align__(16) uint8_t img[];
+  for (int64_t bi = blockIdx.x; bi < nbricks; bi += gridDim.x) {
+    const int rbk = bricks[2 * bi], kbk = bricks[2 * bi + 1];
+    for (int e = threadIdx.x; e < ROWS * BK; e += blockDim.x) {
+      int r, k;
+      if (v.row_contig) {
+        r = e % ROWS;
+        k = e / ROWS;
+      } else {
+        k = e % BK;
+        r = e / BK;
+      }
+      const int64_t gr = (int64_t)rbk * ROWS + r, gk = (int64_t)kbk * BK + k;
+      double x = 0.0;
+      int frame = 0;
+      if (gr < rows_total && gk < k_total) {
+        const int rt = row_tile[gr], kt = k_tile[gk];
+        const int64_t o = v.off[(int64_t)rt * v.off_stride_row + (int64_t)kt * v.off_stride_k];
+        if (o >= 0) {
+          const int lr = row_local[gr], lk = k_local[gk];
+          const int m = v.rsz[rt], kk = v.ksz[kt];
+          x = v.row_contig ? v.data[o + (int64_t)lk * m + lr] : v.data[o + (int64_t)lr * kk + lk];
+        }
+        frame = E[gr];
+      }
+      // fixed point: round(x * 2^(8S-1-E)), E = frame - 1022
+      int64_t fx = 0;
+      const uint64_t bits = (uint64_t)__double_as_longlong(x);
+      const int be = (int)((bits >> 52) & 0x7ff);
+      if (frame > 0 && (bits << 1) != 0) {
+        uint64_t mant = bits & 0xFFFFFFFFFFFFFull;
+        int bexp = be;
+        if (be == 0) {
+          bexp = 1;  // subnormal
+        } else {
+          mant |= 1ull << 52;
+        }
+        const int E = frame - 1022;
+        const int sh = 1075 + E - (8 * S - 1) - bexp;   // >= 53 - (8S - 1) >= 0 for S <= 6
+        uint64_t q;
+        if (sh <= 0) {
+          q = mant << (-sh);
+        } else if (sh >= 64) {
+          q = 0;
+        } else {
+          q = (mant >> sh) + ((mant >> (sh - 1)) & 1ull);  // round half up in magnitude
+        }
+        fx = (bits >> 63) ? -(int64_t)q : (int64_t)q;
+      }
+      // balanced base-256 digits, least significant first
+      int dig[S];
+#pragma unroll
+      for (int p = S - 1; p >= 1; --p) {
+        const int d = (int)(((fx + 128) & 255) - 128);
+        dig[p] = d;
+        fx = (fx - d) >> 8;
+      }
+      dig[0] = (int)fx;
+      const uint32_t bo = brick_offset(r, k);
+#pragma unroll
+      for (int p = 0; p < S; ++p)
+        *reinterpret_cast<uint16_t*>(img + p * SLICE + bo) =
+            (uint16_t)(__float_as_uint((float)dig[p]) >> 16);  // exact: |d| <= 128
+    }
+    __syncthreads();
+    uint4* dst = reinterpret_cast<uint4*>(pack + (size_t)bi * S * SLICE);
+    const uint4* src = reinterpret_cast<const uint4*>(img);
+    for (int i = threadIdx.x; i < S * SLICE / 16; i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+  }
+}
+
+// Does any present tile overlap brick (row block, k block)?
+__global__ void brick_flag_kernel(OperandView v, const int32_t* __restrict__ row_tile,
+                                  const int32_t* __restrict__ k_tile, int64_t rows_total,
+                                  int64_t k_total, int ROWS, int64_t RB, int64_t KB,
+                                  int64_t* __restrict__ flag) {
+  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= RB * KB) return;
+  const int64_t rb = x / KB, kb = x - (x / KB) * KB;
+  const int64_t r0 = rb * ROWS, r1 = min(rows_total, r0 + ROWS) - 1;
+  const int64_t k0 = kb * BK, k1 = min(k_total, k0 + BK) - 1;
+  int64_t f = 0;
+  for (int rt = row_tile[r0]; rt <= row_tile[r1] && !f; ++rt)
+    for (int kt = k_tile[k0]; kt <= k_tile[k1]; ++kt)
+      if (v.off[(int64_t)rt * v.off_stride_row + (int64_t)kt * v.off_stride_k] >= 0) {
+        f = 1;
+        break;
+      }
+  flag[x] = f;
+}
+
+__global__ void brick_slot_kernel(const int64_t* __restrict__ flag,
+                                  const int64_t* __restrict__ scan, int64_t n, int64_t KB,
+                                  int32_t* __restrict__ slot, int32_t* __restrict__ list) {
+  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n) return;
+  if (flag[x]) {
+    const int64_t s = scan[x];
+    slot[x] = (int32_t)s;
+    list[2 * s] = (int32_t)(x / KB);
+    list[2 * s + 1] = (int32_t)(x - (x / KB) * KB);
+  } else {
+    slot[x] = -1;
+  }
+}
+
+// One warp per output block: active if it overlaps a nonzero result tile;
+// count (emit) the k blocks whose A and B bricks both exist.
+__global__ void block_kernel(const int32_t* __restrict__ brickA, const int32_t* __restrict__ brickB,
+                             const int32_t* __restrict__ row_tile,
+                             const int32_t* __restrict__ col_tile, const int64_t* __restrict__ coff,
+                             int64_t Nt, int64_t M_total, int64_t N_total, int64_t RB, int64_t CB,
+                             int64_t KB, const int64_t* __restrict__ offs /* null: count */,
+                             int64_t* __restrict__ counts, int32_t* __restrict__ kbs) {
+  const int lane = threadIdx.x & 31;
+  const int64_t x = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (x >= RB * CB) return;
+  const int64_t rb = x / CB, cb = x - (x / CB) * CB;
+  const int64_t r0 = rb * BM, r1 = min(M_total, r0 + BM) - 1;
+  const int64_t c0 = cb * BN, c1 = min(N_total, c0 + BN) - 1;
+  bool active = false;
+  for (int it = row_tile[r0]; it <= row_tile[r1] && !active; ++it)
+    for (int jt = col_tile[c0]; jt <= col_tile[c1]; ++jt)
+      if (coff[(int64_t)it * Nt + jt] >= 0) {
+        active = true;
+        break;
+      }
+  int64_t cnt = 0;
+  int64_t pos = offs ? offs[x] : 0;
+  if (active) {
+    for (int64_t k0 = 0; k0 < KB; k0 += 32) {
+      const int64_t kb = k0 + lane;
+      const bool p = kb < KB && brickA[rb * KB + kb] >= 0 && brickB[kb * CB + cb] >= 0;
+      const unsigned bm = __ballot_sync(0xffffffffu, p);
+      if (offs && p) kbs[pos + __popc(bm & ((1u << lane) - 1u))] = (int32_t)kb;
+      pos += __popc(bm);
+      cnt += __popc(bm);
+    }
+  }
+  if (!offs && lane == 0) counts[x] = cnt;
+}
+
+__global__ void block_list_kernel(const int64_t* __restrict__ counts,
+                                  const int64_t* __restrict__ scan_blocks, int64_t n, int64_t CB,
+                                  int32_t* __restrict__ blk) {
+  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n || counts[x] == 0) return;
+  const int64_t s = scan_blocks[x];
+  blk[2 * s] = (int32_t)(x / CB);
+  blk[2 * s + 1] = (int32_t)(x - (x / CB) * CB);
+}
+
+__global__ void flag_nonzero_kernel(const int64_t* __restrict__ counts, int64_t n,
+                                    int64_t* __restrict__ flag) {
+  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x < n) flag[x] = counts[x] > 0 ? 1 : 0;
+}
+
+__global__ void gather_offsets_kernel(const int64_t* __restrict__ counts,
+                                      const int64_t* __restrict__ scan_counts,
+                                      const int64_t* __restrict__ scan_blocks, int64_t n,
+                                      int64_t* __restrict__ blk_off) {
+  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n) return;
+  if (counts[x] > 0) blk_off[scan_blocks[x]] = scan_counts[x];
+  if (x == n - 1) blk_off[scan_blocks[n]] = scan_counts[n];
+}
+
+inline unsigned blocks_for(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+struct DevVec {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+// All device state of one emulated contraction (scratch).
+struct OzakiPlan {
+  cudaStream_t s = nullptr;
+  int S = 6;
+  int64_t M_total = 0, N_total = 0, K_total = 0;
+  int64_t RB = 0, KB = 0, CB = 0;
+  int64_t nA = 0, nB = 0, nblk = 0, nkb = 0;
+  OperandView va{}, vb{};
+  std::vector<DevVec> bufs;
+  int32_t *row_tile = nullptr, *row_local = nullptr, *k_tile = nullptr, *k_local = nullptr,
+          *col_tile = nullptr, *col_local = nullptr, *rstart = nullptr, *cstart = nullptr;
+  int32_t *EA = nullptr, *EB = nullptr, *brickA = nullptr, *brickB = nullptr, *listA = nullptr,
+          *listB = nullptr, *blk = nullptr, *blk_kb = nullptr;
+  int64_t *blk_off = nullptr, *workA = nullptr, *workB = nullptr;
+  int64_t nworkA = 0, nworkB = 0;
+  uint8_t *Apack = nullptr, *Bpack = nullptr;
+  int* err = nullptr;
+  OzParams P{};
+  size_t bytes = 0;
+  ~OzakiPlan() {
+    for (auto& b : bufs)
+      if (b.p) cudaFreeAsync(b.p, s);
+  }
+  template <typename T>
+  tagpu_status alloc(T** p, size_t n, std::string* e) {
+    void* q = nullptr;
+    const size_t bytes_ = std::max<size_t>(1, n) * sizeof(T);
+    cudaError_t ce = cudaMallocAsync(&q, bytes_, s);
+    if (ce != cudaSuccess) {
+      cudaGetLastError();
+      *e = std::string("ozaki scratch allocation failed: ") + cudaGetErrorString(ce);
+      return TAGPU_ERR_NOMEM;
+    }
+    bufs.push_back({q, bytes_});
+    bytes += bytes_;
+    *p = static_cast<T*>(q);
+    return TAGPU_OK;
+  }
+  template <typename T>
+  tagpu_status upload(T** p, const std::vector<T>& v, std::string* e) {
+    tagpu_status st = alloc(p, v.size(), e);
+    if (st) return st;
+    if (!v.empty()) cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+    return TAGPU_OK;
+  }
+};
+
+namespace {
+
+template <int S>
+void launch_gemm_t(const OzakiPlan& pl, int sm_count) {
+  const size_t smem = Smem<S>::kBytes;
+  static bool set = false;
+  if (!set) {
+    cudaFuncSetAttribute(ozaki_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    set = true;
+  }
+  const int64_t grid = std::min<int64_t>(pl.nblk, sm_count);
+  if (grid > 0) ozaki_gemm_kernel<S><<<(unsigned)grid, THREADS, smem, pl.s>>>(pl.P);
+}
+
+template <int S>
+void launch_split_t(const OzakiPlan& pl, int sm_count) {
+  const int grid_a = (int)std::min<int64_t>(pl.nA, (int64_t)sm_count * 8);
+  const int grid_b = (int)std::min<int64_t>(pl.nB, (int64_t)sm_count * 8);
+  static bool set = false;
+  if (!set) {
+    cudaFuncSetAttribute(split_kernel<S, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         S * A_SLICE_BYTES);
+    cudaFuncSetAttribute(split_kernel<S, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         S * B_SLICE_BYTES);
+    set = true;
+  }
+  if (grid_a > 0)
+    split_kernel<S, BM><<<grid_a, 256, S * A_SLICE_BYTES, pl.s>>>(pl.va, pl.row_tile, pl.row_local, pl.k_tile,
+                                                  pl.k_local, pl.EA, pl.M_total, pl.K_total,
+                                                  pl.listA, pl.nA, pl.Apack);
+  if (grid_b > 0)
+    split_kernel<S, BN><<<grid_b, 256, S * B_SLICE_BYTES, pl.s>>>(pl.vb, pl.col_tile, pl.col_local, pl.k_tile,
+                                                  pl.k_local, pl.EB, pl.N_total, pl.K_total,
+                                                  pl.listB, pl.nB, pl.Bpack);
+}
+
+void index_maps(const int32_t* sz, int64_t n, std::vector<int32_t>& tile,
+                std::vector<int32_t>& local, std::vector<int32_t>& start) {
+  tile.clear();
+  local.clear();
+  start.assign(n + 1, 0);
+  for (int64_t t = 0; t < n; ++t) {
+    start[t + 1] = start[t] + sz[t];
+    for (int32_t x = 0; x < sz[t]; ++x) {
+      tile.push_back((int32_t)t);
+      local.push_back(x);
+    }
+  }
+}
+
+}  // namespace
+
+// Plan: index maps, brick maps, block lists, scratch.  Host reads back only
+// the counts that size the allocations.
+tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
+                        const int32_t* h_nsz, const int32_t* h_ksz, int slices,
+                        OzakiPlan** out, std::string* err) {
+  if (slices < 2 || slices > 7) {
+    *err = "emulated form supports 2..7 slices";
+    return TAGPU_ERR_INVALID;
+  }
+  auto pl = std::make_unique<OzakiPlan>();
+  pl->s = s;
+  pl->S = slices;
+  std::vector<int32_t> rt, rl, rs, kt_, kl, ks, ct, cl, cs;
+  index_maps(h_msz, v.Mt, rt, rl, rs);
+  index_maps(h_ksz, v.Kt, kt_, kl, ks);
+  index_maps(h_nsz, v.Nt, ct, cl, cs);
+  pl->M_total = (int64_t)rt.size();
+  pl->K_total = (int64_t)kt_.size();
+  pl->N_total = (int64_t)ct.size();
+  if (pl->M_total == 0 || pl->N_total == 0 || pl->K_total == 0) {
+    *err = "empty GEMM";
+    return TAGPU_ERR_INVALID;
+  }
+  if (pl->K_total > (1ll << 18)) {
+    *err = "emulated form: contracted extent above 262144 (the top level would leave the "
+           "exact fp32 range)";
+    return TAGPU_ERR_UNSUPPORTED;
+  }
+  pl->RB = (pl->M_total + BM - 1) / BM;
+  pl->CB = (pl->N_total + BN - 1) / BN;
+  pl->KB = (pl->K_total + BK - 1) / BK;
+  tagpu_status st;
+  if ((st = pl->upload(&pl->row_tile, rt, err)) || (st = pl->upload(&pl->row_local, rl, err)) ||
+      (st = pl->upload(&pl->rstart, rs, err)) || (st = pl->upload(&pl->k_tile, kt_, err)) ||
+      (st = pl->upload(&pl->k_local, kl, err)) || (st = pl->upload(&pl->col_tile, ct, err)) ||
+      (st = pl->upload(&pl->col_local, cl, err)) || (st = pl->upload(&pl->cstart, cs, err)) ||
+      (st = pl->alloc(&pl->EA, pl->M_total, err)) || (st = pl->alloc(&pl->EB, pl->N_total, err)) ||
+      (st = pl->alloc(&pl->err, 1, err)))
+    return st;
+  // operand views in (rows, k) form
+  OperandView& a = pl->va;
+  a.data = v.A;
+  a.off = v.aoff;
+  a.rowt = v.Mt;
+  a.kt = v.Kt;
+  a.off_stride_row = v.Kt;
+  a.off_stride_k = 1;
+  a.rsz = v.msz;
+  a.ksz = v.ksz;
+  a.row_contig = v.a_trans;  // trans: tile stored k x m, rows contiguous
+  OperandView& b = pl->vb;
+  b.data = v.B;
+  b.off = v.boff;
+  b.rowt = v.Nt;
+  b.kt = v.Kt;
+  b.off_stride_row = 1;       // boff index = k * Nt + n
+  b.off_stride_k = v.Nt;
+  b.rsz = v.nsz;
+  b.ksz = v.ksz;
+  b.row_contig = v.b_trans ? 0 : 1;  // k x n storage: rows (n) contiguous
+  // frame work lists (tile, local row) on the host from the offsets
+  std::vector<int64_t> aoff_h(v.Mt * v.Kt), boff_h(v.Kt * v.Nt);
+  cudaMemcpyAsync(aoff_h.data(), v.aoff, aoff_h.size() * 8, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(boff_h.data(), v.boff, boff_h.size() * 8, cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  std::vector<int64_t> wa, wb;
+  for (int64_t i = 0; i < v.Mt; ++i)
+    for (int64_t k = 0; k < v.Kt; ++k)
+      if (aoff_h[i * v.Kt + k] >= 0)
+        for (int32_t r = 0; r < h_msz[i]; ++r) wa.push_back(((i * v.Kt + k) << 20) | r);
+  for (int64_t j = 0; j < v.Nt; ++j)
+    for (int64_t k = 0; k < v.Kt; ++k)
+      if (boff_h[k * v.Nt + j] >= 0)
+        for (int32_t r = 0; r < h_nsz[j]; ++r) wb.push_back(((j * v.Kt + k) << 20) | r);
+  pl->nworkA = (int64_t)wa.size();
+  pl->nworkB = (int64_t)wb.size();
+  if ((st = pl->upload(&pl->workA, wa, err)) || (st = pl->upload(&pl->workB, wb, err))) return st;
+  // brick maps
+  int64_t* flag = nullptr;
+  int64_t* scan = nullptr;
+  const int64_t nfa = pl->RB * pl->KB, nfb = pl->CB * pl->KB;
+  const int64_t nf = std::max(nfa, nfb);
+  if ((st = pl->alloc(&flag, nf, err)) || (st = pl->alloc(&scan, nf + 1, err)) ||
+      (st = pl->alloc(&pl->brickA, nfa, err)) || (st = pl->alloc(&pl->listA, 2 * nfa, err)) ||
+      (st = pl->alloc(&pl->brickB, nfb, err)) || (st = pl->alloc(&pl->listB, 2 * nfb, err)))
+    return st;
+  brick_flag_kernel<<<blocks_for(nfa, 256), 256, 0, s>>>(a, pl->row_tile, pl->k_tile, pl->M_total,
+                                                         pl->K_total, BM, pl->RB, pl->KB, flag);
+  launch_exclusive_scan(s, flag, nfa, scan);
+  brick_slot_kernel<<<blocks_for(nfa, 256), 256, 0, s>>>(flag, scan, nfa, pl->KB, pl->brickA,
+                                                         pl->listA);
+  cudaMemcpyAsync(&pl->nA, scan + nfa, 8, cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  // B bricks are indexed (k block, column block) in the GEMM; the flag pass
+  // runs over (column block, k block) and is transposed into brickB
+  {
+    int32_t* slot_cb = nullptr;
+    if ((st = pl->alloc(&slot_cb, nfb, err))) return st;
+    brick_flag_kernel<<<blocks_for(nfb, 256), 256, 0, s>>>(b, pl->col_tile, pl->k_tile,
+                                                           pl->N_total, pl->K_total, BN, pl->CB,
+                                                           pl->KB, flag);
+    launch_exclusive_scan(s, flag, nfb, scan);
+    brick_slot_kernel<<<blocks_for(nfb, 256), 256, 0, s>>>(flag, scan, nfb, pl->KB, slot_cb,
+                                                           pl->listB);
+    cudaMemcpyAsync(&pl->nB, scan + nfb, 8, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    std::vector<int32_t> h(nfb), t(nfb);
+    cudaMemcpyAsync(h.data(), slot_cb, nfb * 4, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    for (int64_t cb = 0; cb < pl->CB; ++cb)
+      for (int64_t kb = 0; kb < pl->KB; ++kb) t[kb * pl->CB + cb] = h[cb * pl->KB + kb];
+    cudaMemcpyAsync(pl->brickB, t.data(), nfb * 4, cudaMemcpyHostToDevice, s);
+  }
+  // output blocks and their k-block lists
+  const int64_t nob = pl->RB * pl->CB;
+  int64_t *counts = nullptr, *scan_c = nullptr, *bflag = nullptr, *scan_b = nullptr;
+  if ((st = pl->alloc(&counts, nob, err)) || (st = pl->alloc(&scan_c, nob + 1, err)) ||
+      (st = pl->alloc(&bflag, nob, err)) || (st = pl->alloc(&scan_b, nob + 1, err)))
+    return st;
+  block_kernel<<<blocks_for(nob * 32, 256), 256, 0, s>>>(
+      pl->brickA, pl->brickB, pl->row_tile, pl->col_tile, v.coff, v.Nt, pl->M_total, pl->N_total,
+      pl->RB, pl->CB, pl->KB, nullptr, counts, nullptr);
+  launch_exclusive_scan(s, counts, nob, scan_c);
+  flag_nonzero_kernel<<<blocks_for(nob, 256), 256, 0, s>>>(counts, nob, bflag);
+  launch_exclusive_scan(s, bflag, nob, scan_b);
+  cudaMemcpyAsync(&pl->nkb, scan_c + nob, 8, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(&pl->nblk, scan_b + nob, 8, cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  if ((st = pl->alloc(&pl->blk, 2 * pl->nblk, err)) ||
+      (st = pl->alloc(&pl->blk_off, pl->nblk + 1, err)) ||
+      (st = pl->alloc(&pl->blk_kb, pl->nkb, err)))
+    return st;
+  block_kernel<<<blocks_for(nob * 32, 256), 256, 0, s>>>(
+      pl->brickA, pl->brickB, pl->row_tile, pl->col_tile, v.coff, v.Nt, pl->M_total, pl->N_total,
+      pl->RB, pl->CB, pl->KB, scan_c, counts, pl->blk_kb);
+  block_list_kernel<<<blocks_for(nob, 256), 256, 0, s>>>(counts, scan_b, nob, pl->CB, pl->blk);
+  gather_offsets_kernel<<<blocks_for(nob, 256), 256, 0, s>>>(counts, scan_c, scan_b, nob,
+                                                             pl->blk_off);
+  // operand slices
+  const size_t a_brick = (size_t)slices * A_SLICE_BYTES, b_brick = (size_t)slices * B_SLICE_BYTES;
+  if ((st = pl->alloc(&pl->Apack, a_brick * pl->nA, err)) ||
+      (st = pl->alloc(&pl->Bpack, b_brick * pl->nB, err)))
+    return st;
+  cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) {
+    *err = std::string("ozaki planning: ") + cudaGetErrorString(ce);
+    return TAGPU_ERR_CUDA;
+  }
+  OzParams& P = pl->P;
+  P.Apack = pl->Apack;
+  P.Bpack = pl->Bpack;
+  P.brickA = pl->brickA;
+  P.brickB = pl->brickB;
+  P.blk = pl->blk;
+  P.blk_off = pl->blk_off;
+  P.blk_kb = pl->blk_kb;
+  P.nblk = pl->nblk;
+  P.KBn = (int)pl->KB;
+  P.CB = (int)pl->CB;
+  P.EA = pl->EA;
+  P.EB = pl->EB;
+  P.row_tile = pl->row_tile;
+  P.row_local = pl->row_local;
+  P.col_tile = pl->col_tile;
+  P.col_local = pl->col_local;
+  P.nsz = v.nsz;
+  P.Nt = v.Nt;
+  P.coff = v.coff;
+  P.alpha = v.alpha;
+  P.C = v.C;
+  P.M_total = pl->M_total;
+  P.N_total = pl->N_total;
+  P.err = pl->err;
+  *out = pl.release();
+  return TAGPU_OK;
+}
+
+// Frames, splitting and the GEMM; no host synchronisation.
+void ozaki_enqueue(OzakiPlan* pl, int sm_count) {
+  cudaStream_t s = pl->s;
+  cudaMemsetAsync(pl->EA, 0, pl->M_total * 4, s);
+  cudaMemsetAsync(pl->EB, 0, pl->N_total * 4, s);
+  cudaMemsetAsync(pl->err, 0, 4, s);
+  if (pl->nworkA)
+    frame_kernel<<<blocks_for(pl->nworkA * 32, 256), 256, 0, s>>>(pl->va, pl->rstart, pl->workA,
+                                                                   pl->nworkA, pl->EA);
+  if (pl->nworkB)
+    frame_kernel<<<blocks_for(pl->nworkB * 32, 256), 256, 0, s>>>(pl->vb, pl->cstart, pl->workB,
+                                                                   pl->nworkB, pl->EB);
+  switch (pl->S) {
+    case 2: launch_split_t<2>(*pl, sm_count); break;
+    case 3: launch_split_t<3>(*pl, sm_count); break;
+    case 4: launch_split_t<4>(*pl, sm_count); break;
+    case 5: launch_split_t<5>(*pl, sm_count); break;
+    case 6: launch_split_t<6>(*pl, sm_count); break;
+    default: launch_split_t<7>(*pl, sm_count); break;
+  }
+}
+
+void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count) {
+  switch (pl->S) {
+    case 2: launch_gemm_t<2>(*pl, sm_count); break;
+    case 3: launch_gemm_t<3>(*pl, sm_count); break;
+    case 4: launch_gemm_t<4>(*pl, sm_count); break;
+    case 5: launch_gemm_t<5>(*pl, sm_count); break;
+    case 6: launch_gemm_t<6>(*pl, sm_count); break;
+    default: launch_gemm_t<7>(*pl, sm_count); break;
+  }
+}
+
+int ozaki_error(OzakiPlan* pl) {
+  int e = 0;
+  cudaMemcpyAsync(&e, pl->err, 4, cudaMemcpyDeviceToHost, pl->s);
+  cudaStreamSynchronize(pl->s);
+  return e;
+}
+
+size_t ozaki_scratch_bytes(const OzakiPlan* pl) { return pl->bytes; }
+int64_t ozaki_blocks(const OzakiPlan* pl) { return pl->nblk; }
+void ozaki_destroy(OzakiPlan* pl) { delete pl; }
 
 }  // namespace tagpu

@@ -45,6 +45,7 @@ struct tagpu_ctx {
   std::string err;
   tagpu_contract_stats last{};
   std::recursive_mutex mu;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
 };
 
 struct tagpu_array {
@@ -494,6 +495,8 @@ tagpu_status tagpu_shutdown(tagpu_ctx* ctx) {
   if (!ctx) return TAGPU_ERR_INVALID;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  if (ctx->t0) cudaEventDestroy(ctx->t0);
+  if (ctx->t1) cudaEventDestroy(ctx->t1);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return TAGPU_OK;
@@ -504,6 +507,30 @@ const char* tagpu_last_error(const tagpu_ctx* ctx) { return ctx ? ctx->err.c_str
 tagpu_status tagpu_sync(tagpu_ctx* ctx) {
   if (!ctx) return TAGPU_ERR_INVALID;
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_timer_start(tagpu_ctx* ctx) {
+  if (!ctx) return TAGPU_ERR_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  if (!ctx->t0) {
+    CUDA_TRY(ctx, cudaEventCreate(&ctx->t0));
+    CUDA_TRY(ctx, cudaEventCreate(&ctx->t1));
+  }
+  CUDA_TRY(ctx, cudaEventRecord(ctx->t0, ctx->stream));
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_timer_stop(tagpu_ctx* ctx, double* ms) {
+  if (!ctx || !ms || !ctx->t0) return TAGPU_ERR_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  CUDA_TRY(ctx, cudaEventRecord(ctx->t1, ctx->stream));
+  CUDA_TRY(ctx, cudaEventSynchronize(ctx->t1));
+  float f = 0;
+  CUDA_TRY(ctx, cudaEventElapsedTime(&f, ctx->t0, ctx->t1));
+  *ms = f;
   return TAGPU_OK;
 }
 
@@ -847,11 +874,22 @@ struct Contraction {
   double* post_in = nullptr;            // GEMM-order result
   double* post_out = nullptr;           // target-order result
   tagpu_contract_stats st{};
+  OzakiPlan* oz = nullptr;              // emulated form scratch
+  size_t oz_bytes = 0;
   explicit Contraction(tagpu_ctx* c)
       : ctx(c), d_msz(c), d_nsz(c), d_ksz(c), d_aoff(c), d_boff(c), d_poff(c), d_kidx(c),
         d_coff(c) {}
+  ~Contraction();
   tagpu_array* result() { return Cfinal ? Cfinal.get() : C.get(); }
+  bool emulated() const { return precision == TAGPU_PRECISION_OZAKI && oz != nullptr; }
 };
+
+Contraction::~Contraction() {
+  if (oz) {
+    ozaki_destroy(oz);
+    ctx->used -= oz_bytes;
+  }
+}
 
 }  // namespace tagpu
 
@@ -1158,7 +1196,20 @@ tagpu_status plan_all(Contraction& c, const char* c_idx, double alpha, tagpu_arr
   if ((e = make_result(c, A, B))) return e;
   if ((e = prepare_operands(c, A, B))) return e;
   c.view = gemm_view(c);
-  if ((e = build_dmma_items(c, 0))) return e;
+  if (c.precision == TAGPU_PRECISION_OZAKI && c.npairs > 0 && c.C->elements > 0) {
+    std::string err;
+    e = ozaki_plan(ctx->stream, c.view, c.msz.data(), c.nsz.data(), c.ksz.data(), c.slices,
+                   &c.oz, &err);
+    if (e) return fail(ctx, e, "%s", err.c_str());
+    c.oz_bytes = ozaki_scratch_bytes(c.oz);
+    ctx->used += c.oz_bytes;
+    if (ctx->budget && ctx->used.load() > ctx->budget)
+      return fail(ctx, TAGPU_ERR_NOMEM, "emulated-form scratch (%zu bytes) exceeds the budget",
+                  c.oz_bytes);
+    c.st.gemm_blocks = ozaki_blocks(c.oz);
+  } else {
+    if ((e = build_dmma_items(c, 0))) return e;
+  }
   if (c.post) {
     c.post_in = c.C->data;
     c.post_out = c.Cfinal->data;
@@ -1210,8 +1261,8 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, DBuf& 
   std::vector<GemmView> views;
   std::vector<WorkItem> items;
   for (auto* c : cs) {
-    if (c->view.C == nullptr) continue;
-    if (c->precision == TAGPU_PRECISION_FP64 || c->npairs == 0) {
+    if (c->view.C == nullptr || c->emulated()) continue;
+    {
       const int32_t vid = (int32_t)views.size();
       views.push_back(c->view);
       for (WorkItem w : c->items) {
@@ -1225,20 +1276,16 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, DBuf& 
     if ((e = upload_vec(ctx, d_views, views)) || (e = upload_vec(ctx, d_items, items))) return e;
   }
   for (auto* c : cs) {
-    if (c->view.C == nullptr || c->precision == TAGPU_PRECISION_FP64 || c->npairs == 0) continue;
-    const GemmView& v = c->view;
-    size_t scratch = 0;
-    std::string err;
-    tagpu_status e = ozaki_run(ctx->stream, v, c->slices, ctx->sm_count, &scratch,
-                               &c->st.ms_split, &c->st.ms_gemm, &c->st.gemm_blocks, &err);
-    if (e) return fail(ctx, e, "%s", err.c_str());
-    c->st.gemm_launches += 3;
+    if (!c->emulated()) continue;
+    ozaki_enqueue(c->oz, ctx->sm_count);
+    ozaki_enqueue_gemm(c->oz, ctx->sm_count);
+    c->st.gemm_launches = 5;
   }
   if (!items.empty()) {
     launch_dmma_gemm(ctx->stream, d_views.as<GemmView>(), d_items.as<WorkItem>(),
                      (int64_t)items.size(), ctx->sm_count);
     for (auto* c : cs) {
-      if (c->precision != TAGPU_PRECISION_FP64 && c->npairs > 0) continue;
+      if (c->emulated()) continue;
       c->st.gemm_blocks = (int64_t)c->items.size();
       c->st.gemm_launches = c->items.empty() ? 0 : 1;
     }
@@ -1259,12 +1306,29 @@ tagpu_status contract_impl(tagpu_ctx* ctx, const char* c_idx, double alpha, tagp
   if (e) return e;
   DBuf dv(ctx), di(ctx);
   std::vector<Contraction*> cs{&c};
-  {
+  if (c.emulated()) {
+    EventTimer t_split(ctx->stream);
+    ozaki_enqueue(c.oz, ctx->sm_count);
+    t_split.stop();
+    EventTimer t_gemm(ctx->stream);
+    ozaki_enqueue_gemm(c.oz, ctx->sm_count);
+    t_gemm.stop();
+    if (c.post) c.post->enqueue(ctx->stream, c.post_in, c.post_out);
+    CUDA_TRY(ctx, cudaGetLastError());
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    c.st.ms_split = t_split.ms();
+    c.st.ms_gemm = t_gemm.ms();
+    c.st.gemm_launches = 5;
+    const int oe = ozaki_error(c.oz);
+    if (oe)
+      return fail(ctx, TAGPU_ERR_TIMEOUT,
+                  "emulated GEMM: a bounded wait ran out (role code %d); results invalid", oe);
+  } else {
     EventTimer tm(ctx->stream);
     if ((e = enqueue_gemms(ctx, cs, dv, di, true))) return e;
     tm.stop();
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    if (c.precision == TAGPU_PRECISION_FP64 || c.npairs == 0) c.st.ms_gemm = tm.ms();
+    c.st.ms_gemm = tm.ms();
   }
   fill_stats(c);
   c.st.ms_total =
@@ -1366,25 +1430,21 @@ tagpu_status tagpu_batch_run(tagpu_batch* b) {
       Contraction& c = *en.plan;
       fill_stats(c);
     }
-    bool has_ozaki = false;
-    for (auto* c : cs) has_ozaki |= c->precision == TAGPU_PRECISION_OZAKI && c->npairs > 0;
-    if (has_ozaki) {
-      // the emulated form plans its own scratch; run it eagerly
-      if ((e = enqueue_gemms(ctx, cs, b->d_views, b->d_items, true))) return e;
-    } else {
-      // upload views/items first (outside capture), then capture the launches
-      if ((e = enqueue_gemms(ctx, cs, b->d_views, b->d_items, true))) return e;
-      CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-      CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      e = enqueue_gemms(ctx, cs, b->d_views, b->d_items, false);
-      cudaGraph_t g = nullptr;
-      cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
-      if (e) return e;
-      if (ce != cudaSuccess) return fail(ctx, TAGPU_ERR_CUDA, "graph capture failed: %s",
-                                         cudaGetErrorString(ce));
-      b->graph = g;
-      CUDA_TRY(ctx, cudaGraphInstantiate(&b->exec, g, 0));
-    }
+    // run once eagerly (uploads the work lists), then capture the launches
+    if ((e = enqueue_gemms(ctx, cs, b->d_views, b->d_items, true))) return e;
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    for (auto* c : cs)
+      if (c->emulated() && ozaki_error(c->oz))
+        return fail(ctx, TAGPU_ERR_TIMEOUT, "emulated GEMM: a bounded wait ran out");
+    CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    e = enqueue_gemms(ctx, cs, b->d_views, b->d_items, false);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+    if (e) return e;
+    if (ce != cudaSuccess)
+      return fail(ctx, TAGPU_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
+    b->graph = g;
+    CUDA_TRY(ctx, cudaGraphInstantiate(&b->exec, g, 0));
     // results move into the caller-visible handles; the captured launches
     // keep writing the same device buffers, so a result handle must outlive
     // the runs of its batch
@@ -1392,14 +1452,11 @@ tagpu_status tagpu_batch_run(tagpu_batch* b) {
     b->planned = true;
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   } else {
-    if (b->exec) {
-      CUDA_TRY(ctx, cudaGraphLaunch(b->exec, ctx->stream));
-    } else {
-      std::vector<Contraction*> cs;
-      for (auto& en : b->entries) cs.push_back(en.plan.get());
-      if ((e = enqueue_gemms(ctx, cs, b->d_views, b->d_items, false))) return e;
-    }
+    CUDA_TRY(ctx, cudaGraphLaunch(b->exec, ctx->stream));
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    for (auto& en : b->entries)
+      if (en.plan->emulated() && ozaki_error(en.plan->oz))
+        return fail(ctx, TAGPU_ERR_TIMEOUT, "emulated GEMM: a bounded wait ran out");
   }
   tagpu_contract_stats& s = b->stats;
   s = tagpu_contract_stats{};
