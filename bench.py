@@ -137,31 +137,39 @@ def cpu_sample(A_t, B_t, h, scale, seconds, threads, seed=0):
     rng = np.random.default_rng(seed)
     cand = np.flatnonzero(tile_fl > 0)
     rng.shuffle(cand)
-    # calibrate: ~2 GFLOP/s per core for a first guess, then grow
-    budget = seconds * threads * 8e9
-    sel, acc = [], 0.0
-    for t in cand:
-        sel.append(t)
-        acc += tile_fl[t]
-        if acc >= budget:
-            break
-    sel = np.asarray(sorted(sel), np.int64)
     msz = nsz = ksz = sizes.astype(np.int64)
-    res_off = np.full(nt * nt, -1, np.int64)
-    pos = 0
-    for t in sel:
-        res_off[t] = pos
-        pos += int(sizes[t // nt] * sizes[t % nt])
-    cbuf = np.zeros(max(pos, 1))
     L = O.lib()
     P = lambda a, ty: a.ctypes.data_as(ty)
-    t0 = time.perf_counter()
-    L.orc_contract_subset(nt, nt, nt, P(msz, O._i64p), P(nsz, O._i64p), P(ksz, O._i64p),
-                          P(A_t["data"], O._f64p), P(A_t["offsets"], O._i64p), 0,
-                          P(B_t["data"], O._f64p), P(B_t["offsets"], O._i64p), 0,
-                          P(offs, O._i64p), P(kidx, O._i32p), 1.0, P(cbuf, O._f64p),
-                          P(res_off, O._i64p), P(sel, O._i64p), len(sel), threads, fn)
-    dt = time.perf_counter() - t0
+
+    def run(sel):
+        sel = np.asarray(sorted(sel), np.int64)
+        res_off = np.full(nt * nt, -1, np.int64)
+        pos = 0
+        for t in sel:
+            res_off[t] = pos
+            pos += int(sizes[t // nt] * sizes[t % nt])
+        cbuf = np.zeros(max(pos, 1))
+        t0 = time.perf_counter()
+        L.orc_contract_subset(nt, nt, nt, P(msz, O._i64p), P(nsz, O._i64p), P(ksz, O._i64p),
+                              P(A_t["data"], O._f64p), P(A_t["offsets"], O._i64p), 0,
+                              P(B_t["data"], O._f64p), P(B_t["offsets"], O._i64p), 0,
+                              P(offs, O._i64p), P(kidx, O._i32p), 1.0, P(cbuf, O._f64p),
+                              P(res_off, O._i64p), P(sel, O._i64p), len(sel), threads, fn)
+        return sel, time.perf_counter() - t0
+
+    # calibrate on a small sample, then size the timed sample to `seconds`
+    def take(budget):
+        sel, acc = [], 0.0
+        for t in cand:
+            sel.append(t)
+            acc += tile_fl[t]
+            if acc >= budget:
+                break
+        return sel
+    cal = take(threads * 2e9)
+    csel, cdt = run(cal)
+    rate = tile_fl[csel].sum() / max(cdt, 1e-6)
+    sel, dt = run(take(rate * seconds))
     fl = tile_fl[sel].sum()
     desc = (f"{len(sel)} of {len(cand)} nonzero result tiles ({fl / tile_fl.sum() * 100:.2f}% "
             f"of the flops), per-pair {'OpenBLAS' if fn else 'oracle-loop'} dgemm, {threads} threads")

@@ -216,6 +216,62 @@ tagpu_status tagpu_batch_run(tagpu_batch* b);
 tagpu_status tagpu_batch_stats(const tagpu_batch* b, tagpu_contract_stats* st);
 tagpu_status tagpu_batch_destroy(tagpu_batch* b);
 
+/* ---- serving: continuous batching of contraction requests --------------- */
+typedef struct tagpu_server tagpu_server;
+typedef struct tagpu_server_config {
+  size_t hbm_budget_bytes;    /* admission budget for results and scratch;
+                                 0 = no budget */
+  int max_batch;              /* contractions per launch, 0 = 64 */
+  int precision;              /* default precision of requests */
+  int slices;                 /* default Ozaki slices, 0 = 6 */
+} tagpu_server_config;
+typedef struct tagpu_request {
+  const char* c_idx;
+  double alpha;
+  tagpu_array* A;
+  const char* a_idx;
+  tagpu_array* B;
+  const char* b_idx;
+  int precision;              /* < 0: server default */
+  int slices;                 /* <= 0: server default */
+} tagpu_request;
+typedef struct tagpu_request_result {
+  tagpu_status status;        /* status of the contraction itself */
+  double latency_ms;          /* submit -> result ready */
+  double queue_ms;            /* submit -> admitted */
+  double flops;               /* nonzero-block flops */
+  int64_t pairs;
+  int batch_size;             /* contractions in its launch */
+  uint64_t batch_id;
+} tagpu_request_result;
+typedef struct tagpu_server_stats {
+  int64_t submitted, completed, rejected, failed, batches;
+  double p50_ms, p99_ms, mean_ms; /* latency of completed requests */
+  double flops;               /* total nonzero-block flops completed */
+  double wall_ms;             /* first submit -> last completion */
+  size_t bytes_in_use, peak_bytes;
+} tagpu_server_stats;
+
+/* Starts the request loop on its own host thread.  Requests reference arrays
+ * that stay resident on the device; a request whose footprint bound exceeds
+ * the budget is rejected at submit (TAGPU_ERR_REJECTED); others wait until
+ * enough of the budget is free and are batched with whatever else is
+ * admitted.  While one batch runs on the GPU the next one is planned. */
+tagpu_status tagpu_server_start(tagpu_ctx* ctx, const tagpu_server_config* cfg,
+                                tagpu_server** out);
+/* Thread-safe. */
+tagpu_status tagpu_server_submit(tagpu_server* s, const tagpu_request* req, uint64_t* id);
+/* TAGPU_ERR_NOT_READY while in flight; on TAGPU_OK *c (may be NULL to drop
+ * it) receives the result array, owned by the caller from then on. */
+tagpu_status tagpu_server_poll(tagpu_server* s, uint64_t id, tagpu_array** c,
+                               tagpu_request_result* res);
+/* Blocks up to timeout_ms (< 0: no limit) then behaves like poll. */
+tagpu_status tagpu_server_wait(tagpu_server* s, uint64_t id, double timeout_ms,
+                               tagpu_array** c, tagpu_request_result* res);
+tagpu_status tagpu_server_get_stats(tagpu_server* s, tagpu_server_stats* st);
+/* Finishes queued work, then stops the loop and frees the server. */
+tagpu_status tagpu_server_stop(tagpu_server* s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,39 @@ class ContractStats(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_batch", ctypes.c_int),
+                ("precision", ctypes.c_int), ("slices", ctypes.c_int)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("c_idx", ctypes.c_char_p), ("alpha", ctypes.c_double), ("A", _vp),
+                ("a_idx", ctypes.c_char_p), ("B", _vp), ("b_idx", ctypes.c_char_p),
+                ("precision", ctypes.c_int), ("slices", ctypes.c_int)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("latency_ms", ctypes.c_double),
+                ("queue_ms", ctypes.c_double), ("flops", ctypes.c_double),
+                ("pairs", ctypes.c_int64), ("batch_size", ctypes.c_int),
+                ("batch_id", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64),
+                ("rejected", ctypes.c_int64), ("failed", ctypes.c_int64),
+                ("batches", ctypes.c_int64), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
+                ("flops", ctypes.c_double), ("wall_ms", ctypes.c_double),
+                ("bytes_in_use", ctypes.c_size_t), ("peak_bytes", ctypes.c_size_t)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 _L = None
 
 # name -> (restype, argtypes); every symbol include/tagpu.h declares
@@ -120,6 +153,15 @@ SIGNATURES = {
     "tagpu_batch_run": (ctypes.c_int, [_vp]),
     "tagpu_batch_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ContractStats)]),
     "tagpu_batch_destroy": (ctypes.c_int, [_vp]),
+    "tagpu_server_start": (ctypes.c_int, [_vp, ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
+    "tagpu_server_submit": (ctypes.c_int, [_vp, ctypes.POINTER(Request),
+                                           ctypes.POINTER(ctypes.c_uint64)]),
+    "tagpu_server_poll": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.POINTER(_vp),
+                                         ctypes.POINTER(RequestResult)]),
+    "tagpu_server_wait": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_double,
+                                         ctypes.POINTER(_vp), ctypes.POINTER(RequestResult)]),
+    "tagpu_server_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)]),
+    "tagpu_server_stop": (ctypes.c_int, [_vp]),
 }
 
 
@@ -453,3 +495,55 @@ def contract(world, c_idx, alpha, A, a_idx, B, b_idx, precision=PRECISION_FP64, 
                                        a_idx.encode(), B.h, b_idx.encode(), ctypes.byref(opts),
                                        ctypes.byref(h)))
     return DistArray(world, _handle=h), world.last_stats()
+
+
+class Server:
+    """Request loop: HBM-footprint admission and continuous batching."""
+
+    def __init__(self, world: World, hbm_budget_bytes=0, max_batch=64,
+                 precision=PRECISION_FP64, slices=6):
+        self.world = world
+        cfg = ServerConfig(hbm_budget_bytes, max_batch, precision, slices)
+        h = _vp()
+        world.check(world.L.tagpu_server_start(world.h, ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+        self._keep = {}
+
+    def submit(self, c_idx, alpha, A, a_idx, B, b_idx, precision=-1, slices=0):
+        """Returns a request id; raises TAGPUError (status 6) on rejection."""
+        req = Request(c_idx.encode(), float(alpha), A.h, a_idx.encode(), B.h, b_idx.encode(),
+                      int(precision), int(slices))
+        rid = ctypes.c_uint64(0)
+        self.world.check(self.world.L.tagpu_server_submit(self.h, ctypes.byref(req),
+                                                           ctypes.byref(rid)))
+        self._keep[rid.value] = (A, B)
+        return rid.value
+
+    def wait(self, rid, timeout_ms=-1.0):
+        c = _vp()
+        res = RequestResult()
+        self.world.check(self.world.L.tagpu_server_wait(self.h, rid, float(timeout_ms),
+                                                         ctypes.byref(c), ctypes.byref(res)))
+        self._keep.pop(rid, None)
+        arr = DistArray(self.world, _handle=c) if c.value else None
+        return arr, res.as_dict()
+
+    def poll(self, rid):
+        c = _vp()
+        res = RequestResult()
+        st = self.world.L.tagpu_server_poll(self.h, rid, ctypes.byref(c), ctypes.byref(res))
+        if st == 7:
+            return None
+        self.world.check(st)
+        self._keep.pop(rid, None)
+        return (DistArray(self.world, _handle=c) if c.value else None), res.as_dict()
+
+    def stats(self):
+        s = ServerStats()
+        self.world.check(self.world.L.tagpu_server_get_stats(self.h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def stop(self):
+        if self.h is not None:
+            self.world.check(self.world.L.tagpu_server_stop(self.h))
+            self.h = None

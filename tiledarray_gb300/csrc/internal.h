@@ -101,8 +101,8 @@ struct OzakiPlan;
 tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
                         const int32_t* h_nsz, const int32_t* h_ksz, int slices,
                         OzakiPlan** out, std::string* err);
-void ozaki_enqueue(OzakiPlan* pl, int sm_count);
-void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count);
+void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s);
+void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s);
 int ozaki_error(OzakiPlan* pl);   // synchronises; 0 = ok
 size_t ozaki_scratch_bytes(const OzakiPlan* pl);
 int64_t ozaki_blocks(const OzakiPlan* pl);

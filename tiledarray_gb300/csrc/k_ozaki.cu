@@ -751,7 +751,7 @@ struct OzakiPlan {
 namespace {
 
 template <int S>
-void launch_gemm_t(const OzakiPlan& pl, int sm_count) {
+void launch_gemm_t(const OzakiPlan& pl, int sm_count, cudaStream_t st) {
   const size_t smem = Smem<S>::kBytes;
   static bool set = false;
   if (!set) {
@@ -760,11 +760,11 @@ void launch_gemm_t(const OzakiPlan& pl, int sm_count) {
     set = true;
   }
   const int64_t grid = std::min<int64_t>(pl.nblk, sm_count);
-  if (grid > 0) ozaki_gemm_kernel<S><<<(unsigned)grid, THREADS, smem, pl.s>>>(pl.P);
+  if (grid > 0) ozaki_gemm_kernel<S><<<(unsigned)grid, THREADS, smem, st>>>(pl.P);
 }
 
 template <int S>
-void launch_split_t(const OzakiPlan& pl, int sm_count) {
+void launch_split_t(const OzakiPlan& pl, int sm_count, cudaStream_t st) {
   const int grid_a = (int)std::min<int64_t>(pl.nA, (int64_t)sm_count * 8);
   const int grid_b = (int)std::min<int64_t>(pl.nB, (int64_t)sm_count * 8);
   static bool set = false;
@@ -776,11 +776,11 @@ void launch_split_t(const OzakiPlan& pl, int sm_count) {
     set = true;
   }
   if (grid_a > 0)
-    split_kernel<S, BM><<<grid_a, 256, S * A_SLICE_BYTES, pl.s>>>(pl.va, pl.row_tile, pl.row_local, pl.k_tile,
+    split_kernel<S, BM><<<grid_a, 256, S * A_SLICE_BYTES, st>>>(pl.va, pl.row_tile, pl.row_local, pl.k_tile,
                                                   pl.k_local, pl.EA, pl.M_total, pl.K_total,
                                                   pl.listA, pl.nA, pl.Apack);
   if (grid_b > 0)
-    split_kernel<S, BN><<<grid_b, 256, S * B_SLICE_BYTES, pl.s>>>(pl.vb, pl.col_tile, pl.col_local, pl.k_tile,
+    split_kernel<S, BN><<<grid_b, 256, S * B_SLICE_BYTES, st>>>(pl.vb, pl.col_tile, pl.col_local, pl.k_tile,
                                                   pl.k_local, pl.EB, pl.N_total, pl.K_total,
                                                   pl.listB, pl.nB, pl.Bpack);
 }
@@ -979,8 +979,7 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
 }
 
 // Frames, splitting and the GEMM; no host synchronisation.
-void ozaki_enqueue(OzakiPlan* pl, int sm_count) {
-  cudaStream_t s = pl->s;
+void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s) {
   cudaMemsetAsync(pl->EA, 0, pl->M_total * 4, s);
   cudaMemsetAsync(pl->EB, 0, pl->N_total * 4, s);
   cudaMemsetAsync(pl->err, 0, 4, s);
@@ -991,23 +990,23 @@ void ozaki_enqueue(OzakiPlan* pl, int sm_count) {
     frame_kernel<<<blocks_for(pl->nworkB * 32, 256), 256, 0, s>>>(pl->vb, pl->cstart, pl->workB,
                                                                    pl->nworkB, pl->EB);
   switch (pl->S) {
-    case 2: launch_split_t<2>(*pl, sm_count); break;
-    case 3: launch_split_t<3>(*pl, sm_count); break;
-    case 4: launch_split_t<4>(*pl, sm_count); break;
-    case 5: launch_split_t<5>(*pl, sm_count); break;
-    case 6: launch_split_t<6>(*pl, sm_count); break;
-    default: launch_split_t<7>(*pl, sm_count); break;
+    case 2: launch_split_t<2>(*pl, sm_count, s); break;
+    case 3: launch_split_t<3>(*pl, sm_count, s); break;
+    case 4: launch_split_t<4>(*pl, sm_count, s); break;
+    case 5: launch_split_t<5>(*pl, sm_count, s); break;
+    case 6: launch_split_t<6>(*pl, sm_count, s); break;
+    default: launch_split_t<7>(*pl, sm_count, s); break;
   }
 }
 
-void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count) {
+void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s) {
   switch (pl->S) {
-    case 2: launch_gemm_t<2>(*pl, sm_count); break;
-    case 3: launch_gemm_t<3>(*pl, sm_count); break;
-    case 4: launch_gemm_t<4>(*pl, sm_count); break;
-    case 5: launch_gemm_t<5>(*pl, sm_count); break;
-    case 6: launch_gemm_t<6>(*pl, sm_count); break;
-    default: launch_gemm_t<7>(*pl, sm_count); break;
+    case 2: launch_gemm_t<2>(*pl, sm_count, s); break;
+    case 3: launch_gemm_t<3>(*pl, sm_count, s); break;
+    case 4: launch_gemm_t<4>(*pl, sm_count, s); break;
+    case 5: launch_gemm_t<5>(*pl, sm_count, s); break;
+    case 6: launch_gemm_t<6>(*pl, sm_count, s); break;
+    default: launch_gemm_t<7>(*pl, sm_count, s); break;
   }
 }
 

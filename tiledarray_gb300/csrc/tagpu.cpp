@@ -17,6 +17,10 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+#include <unordered_map>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -1257,7 +1261,8 @@ namespace tagpu {
 // Kernel (d) and the post-permutation for a set of planned contractions;
 // no host synchronisation, so the sequence can be captured in a graph.
 tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, DBuf& d_views,
-                           DBuf& d_items, bool upload) {
+                           DBuf& d_items, bool upload, cudaStream_t stream = nullptr) {
+  if (!stream) stream = ctx->stream;
   std::vector<GemmView> views;
   std::vector<WorkItem> items;
   for (auto* c : cs) {
@@ -1274,15 +1279,16 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, DBuf& 
   if (upload) {
     tagpu_status e;
     if ((e = upload_vec(ctx, d_views, views)) || (e = upload_vec(ctx, d_items, items))) return e;
+    if (stream != ctx->stream) CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   }
   for (auto* c : cs) {
     if (!c->emulated()) continue;
-    ozaki_enqueue(c->oz, ctx->sm_count);
-    ozaki_enqueue_gemm(c->oz, ctx->sm_count);
+    ozaki_enqueue(c->oz, ctx->sm_count, stream);
+    ozaki_enqueue_gemm(c->oz, ctx->sm_count, stream);
     c->st.gemm_launches = 5;
   }
   if (!items.empty()) {
-    launch_dmma_gemm(ctx->stream, d_views.as<GemmView>(), d_items.as<WorkItem>(),
+    launch_dmma_gemm(stream, d_views.as<GemmView>(), d_items.as<WorkItem>(),
                      (int64_t)items.size(), ctx->sm_count);
     for (auto* c : cs) {
       if (c->emulated()) continue;
@@ -1291,7 +1297,7 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, DBuf& 
     }
   }
   for (auto* c : cs)
-    if (c->post) c->post->enqueue(ctx->stream, c->post_in, c->post_out);
+    if (c->post) c->post->enqueue(stream, c->post_in, c->post_out);
   CUDA_TRY(ctx, cudaGetLastError());
   return TAGPU_OK;
 }
@@ -1308,10 +1314,10 @@ tagpu_status contract_impl(tagpu_ctx* ctx, const char* c_idx, double alpha, tagp
   std::vector<Contraction*> cs{&c};
   if (c.emulated()) {
     EventTimer t_split(ctx->stream);
-    ozaki_enqueue(c.oz, ctx->sm_count);
+    ozaki_enqueue(c.oz, ctx->sm_count, ctx->stream);
     t_split.stop();
     EventTimer t_gemm(ctx->stream);
-    ozaki_enqueue_gemm(c.oz, ctx->sm_count);
+    ozaki_enqueue_gemm(c.oz, ctx->sm_count, ctx->stream);
     t_gemm.stop();
     if (c.post) c.post->enqueue(ctx->stream, c.post_in, c.post_out);
     CUDA_TRY(ctx, cudaGetLastError());
@@ -1628,6 +1634,351 @@ tagpu_status tagpu_permute(tagpu_ctx* ctx, int rank, const int64_t* extents, con
   CUDA_TRY(ctx, cudaMemcpyAsync(out, dout.p, vol * sizeof(double), cudaMemcpyDeviceToHost,
                                 ctx->stream));
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return TAGPU_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// serving: admission by HBM footprint, continuous batching, two-stage pipeline
+// (plan the next batch on the context stream while the GEMMs of the current
+// batch run on the server's own stream)
+// ---------------------------------------------------------------------------
+
+struct tagpu_server {
+  struct Req {
+    uint64_t id = 0;
+    std::string c, a, b;
+    double alpha = 1.0;
+    tagpu_array *A = nullptr, *B = nullptr;
+    tagpu_contract_opts opts{};
+    size_t bound = 0;        // footprint reserved at admission
+    double t_submit = 0, t_admit = 0;
+    bool done = false;
+    tagpu_array* C = nullptr;
+    tagpu_request_result res{};
+    std::unique_ptr<Contraction> plan;
+  };
+  tagpu_ctx* ctx = nullptr;
+  tagpu_server_config cfg{};
+  cudaStream_t gemm_stream = nullptr;
+  std::thread worker;
+  std::mutex m;
+  std::condition_variable cv, done_cv;
+  bool stopping = false;
+  std::deque<std::shared_ptr<Req>> queue;
+  std::unordered_map<uint64_t, std::shared_ptr<Req>> all;
+  uint64_t next_id = 1, next_batch = 1;
+  size_t in_use = 0, peak = 0;
+  int64_t submitted = 0, completed = 0, rejected = 0, failed = 0, batches = 0;
+  double flops = 0, t_first = -1, t_last = 0;
+  std::vector<double> lat;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  double now_ms() const {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
+        .count();
+  }
+  void run();
+};
+
+namespace {
+
+// Upper bound of the device bytes a request can need: the dense result, the
+// pair list, permuted operand copies and the emulated form's digit bricks.
+size_t footprint_bound(tagpu_array* A, const std::vector<std::string>& ai, tagpu_array* B,
+                       const std::vector<std::string>& bi, const tagpu_contract_opts& o) {
+  double m = 1, n = 1, k = 1, mt = 1, nt = 1, kt = 1;
+  for (size_t d = 0; d < ai.size(); ++d) {
+    const double ext = (double)(A->hm[d].back() - A->hm[d][0]);
+    if (find_idx(bi, ai[d]) >= 0) {
+      k *= ext;
+      kt *= (double)A->nt[d];
+    } else {
+      m *= ext;
+      mt *= (double)A->nt[d];
+    }
+  }
+  for (size_t d = 0; d < bi.size(); ++d)
+    if (find_idx(ai, bi[d]) < 0) {
+      n *= (double)(B->hm[d].back() - B->hm[d][0]);
+      nt *= (double)B->nt[d];
+    }
+  double bytes = 2.0 * m * n * 8;                 // result (+ permuted copy)
+  bytes += mt * nt * kt * 4 + mt * nt * 32;       // pair list, offsets
+  bytes += (double)A->bytes + (double)B->bytes;   // explicit permutations
+  if (o.precision == TAGPU_PRECISION_OZAKI) {
+    const int S = o.slices > 0 ? o.slices : 6;
+    const double kk = std::ceil(k / 32.0) * 32.0;
+    bytes += (std::ceil(m / 128.0) * 128.0 + std::ceil(n / 64.0) * 64.0) * kk * 2.0 * S;
+    bytes += (m + n) * 24 + (m / 128.0 + n / 64.0 + 2) * (k / 32.0 + 1) * 32;
+  }
+  return (size_t)bytes + (1u << 20);
+}
+
+}  // namespace
+
+void tagpu_server::run() {
+  std::vector<std::shared_ptr<Req>> inflight;  // GEMMs enqueued on gemm_stream
+  DBuf dv_a(ctx), di_a(ctx), dv_b(ctx), di_b(ctx);
+  bool use_a = true;
+  auto finish_inflight = [&]() {
+    if (inflight.empty()) return;
+    cudaError_t ce = cudaStreamSynchronize(gemm_stream);
+    const double t = now_ms();
+    std::lock_guard<std::mutex> lk(m);
+    for (auto& r : inflight) {
+      Contraction& c = *r->plan;
+      r->res.status = ce == cudaSuccess ? TAGPU_OK : TAGPU_ERR_CUDA;
+      if (r->res.status == TAGPU_OK && c.emulated() && ozaki_error(c.oz))
+        r->res.status = TAGPU_ERR_TIMEOUT;
+      if (r->res.status == TAGPU_OK) {
+        fill_stats(c);
+        r->C = c.Cfinal ? c.Cfinal.release() : c.C.release();
+        r->res.flops = c.flops;
+        r->res.pairs = c.npairs;
+        flops += c.flops;
+        ++completed;
+        lat.push_back(t - r->t_submit);
+      } else {
+        ++failed;
+      }
+      r->res.latency_ms = t - r->t_submit;
+      r->plan.reset();
+      in_use -= r->bound;
+      r->done = true;
+      t_last = t;
+    }
+    inflight.clear();
+    done_cv.notify_all();
+    cv.notify_all();
+  };
+  for (;;) {
+    std::vector<std::shared_ptr<Req>> batch;
+    {
+      std::unique_lock<std::mutex> lk(m);
+      cv.wait(lk, [&] { return stopping || !queue.empty() || !inflight.empty(); });
+      if (stopping && queue.empty() && inflight.empty()) break;
+      const size_t budget = cfg.hbm_budget_bytes;
+      const int maxb = cfg.max_batch > 0 ? cfg.max_batch : 64;
+      for (auto it = queue.begin(); it != queue.end() && (int)batch.size() < maxb;) {
+        if (budget == 0 || in_use + (*it)->bound <= budget) {
+          in_use += (*it)->bound;
+          peak = std::max(peak, in_use);
+          (*it)->t_admit = now_ms();
+          batch.push_back(*it);
+          it = queue.erase(it);
+        } else {
+          ++it;
+        }
+      }
+    }
+    // plan the admitted requests while the previous batch is on the GPU
+    std::vector<Contraction*> cs;
+    std::vector<std::shared_ptr<Req>> ok;
+    {
+      std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+      cudaSetDevice(ctx->device);
+      for (auto& r : batch) {
+        r->plan.reset(new Contraction(ctx));
+        tagpu_status e = plan_all(*r->plan, r->c.c_str(), r->alpha, r->A, r->a.c_str(), r->B,
+                                  r->b.c_str(), &r->opts);
+        if (e) {
+          std::lock_guard<std::mutex> lk2(m);
+          r->res.status = e;
+          r->res.latency_ms = now_ms() - r->t_submit;
+          r->plan.reset();
+          in_use -= r->bound;
+          r->done = true;
+          ++failed;
+          done_cv.notify_all();
+          continue;
+        }
+        cs.push_back(r->plan.get());
+        ok.push_back(r);
+      }
+    }
+    // the previous batch must be done before its buffers are reused
+    finish_inflight();
+    if (!ok.empty()) {
+      std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+      cudaSetDevice(ctx->device);
+      DBuf& dv = use_a ? dv_a : dv_b;
+      DBuf& di = use_a ? di_a : di_b;
+      use_a = !use_a;
+      tagpu_status e = enqueue_gemms(ctx, cs, dv, di, true, gemm_stream);
+      const uint64_t bid = next_batch++;
+      for (auto& r : ok) {
+        r->res.batch_size = (int)ok.size();
+        r->res.batch_id = bid;
+        r->res.queue_ms = r->t_admit - r->t_submit;
+      }
+      ++batches;
+      if (e) {
+        std::lock_guard<std::mutex> lk2(m);
+        for (auto& r : ok) {
+          r->res.status = e;
+          r->plan.reset();
+          in_use -= r->bound;
+          r->done = true;
+          ++failed;
+        }
+        done_cv.notify_all();
+      } else {
+        inflight = ok;
+      }
+    }
+  }
+  finish_inflight();
+}
+
+extern "C" {
+
+tagpu_status tagpu_server_start(tagpu_ctx* ctx, const tagpu_server_config* cfg,
+                                tagpu_server** out) {
+  if (!ctx || !out) return TAGPU_ERR_INVALID;
+  auto* s = new tagpu_server;
+  s->ctx = ctx;
+  if (cfg) s->cfg = *cfg;
+  if (s->cfg.slices <= 0) s->cfg.slices = 6;
+  cudaSetDevice(ctx->device);
+  if (cudaStreamCreateWithFlags(&s->gemm_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete s;
+    return fail(ctx, TAGPU_ERR_CUDA, "server stream creation failed");
+  }
+  s->worker = std::thread([s] {
+    cudaSetDevice(s->ctx->device);
+    s->run();
+  });
+  *out = s;
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_server_submit(tagpu_server* s, const tagpu_request* req, uint64_t* id) {
+  if (!s || !req || !req->A || !req->B || !req->c_idx || !req->a_idx || !req->b_idx)
+    return TAGPU_ERR_INVALID;
+  auto r = std::make_shared<tagpu_server::Req>();
+  r->c = req->c_idx;
+  r->a = req->a_idx;
+  r->b = req->b_idx;
+  r->alpha = req->alpha;
+  r->A = req->A;
+  r->B = req->B;
+  r->opts.precision = req->precision >= 0 ? req->precision : s->cfg.precision;
+  r->opts.slices = req->slices > 0 ? req->slices : s->cfg.slices;
+  r->opts.threshold = -1.0f;
+  std::vector<std::string> ai, bi;
+  if (!parse_indices(req->a_idx, ai) || !parse_indices(req->b_idx, bi) ||
+      (int)ai.size() != req->A->rank || (int)bi.size() != req->B->rank)
+    return fail(s->ctx, TAGPU_ERR_INVALID, "server: malformed request indices");
+  r->bound = footprint_bound(req->A, ai, req->B, bi, r->opts);
+  std::lock_guard<std::mutex> lk(s->m);
+  ++s->submitted;
+  if (s->cfg.hbm_budget_bytes && r->bound > s->cfg.hbm_budget_bytes) {
+    ++s->rejected;
+    return fail(s->ctx, TAGPU_ERR_REJECTED,
+                "request footprint bound %.3g GB exceeds the budget %.3g GB", r->bound / 1e9,
+                s->cfg.hbm_budget_bytes / 1e9);
+  }
+  if (s->stopping) return fail(s->ctx, TAGPU_ERR_STATE, "server is stopping");
+  r->id = s->next_id++;
+  r->t_submit = s->now_ms();
+  if (s->t_first < 0) s->t_first = r->t_submit;
+  s->queue.push_back(r);
+  s->all[r->id] = r;
+  if (id) *id = r->id;
+  s->cv.notify_all();
+  return TAGPU_OK;
+}
+
+static tagpu_status server_take(tagpu_server* s, uint64_t id, tagpu_array** c,
+                                tagpu_request_result* res) {
+  auto it = s->all.find(id);
+  if (it == s->all.end()) return TAGPU_ERR_INVALID;
+  auto r = it->second;
+  if (!r->done) return TAGPU_ERR_NOT_READY;
+  if (res) *res = r->res;
+  if (c) {
+    *c = r->C;
+  } else if (r->C) {
+    std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+    delete r->C;
+  }
+  r->C = nullptr;
+  s->all.erase(it);
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_server_poll(tagpu_server* s, uint64_t id, tagpu_array** c,
+                               tagpu_request_result* res) {
+  if (!s) return TAGPU_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->m);
+  return server_take(s, id, c, res);
+}
+
+tagpu_status tagpu_server_wait(tagpu_server* s, uint64_t id, double timeout_ms, tagpu_array** c,
+                               tagpu_request_result* res) {
+  if (!s) return TAGPU_ERR_INVALID;
+  std::unique_lock<std::mutex> lk(s->m);
+  auto ready = [&] {
+    auto it = s->all.find(id);
+    return it == s->all.end() || it->second->done;
+  };
+  if (timeout_ms < 0) {
+    s->done_cv.wait(lk, ready);
+  } else if (!s->done_cv.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms),
+                                  ready)) {
+    return TAGPU_ERR_TIMEOUT;
+  }
+  return server_take(s, id, c, res);
+}
+
+tagpu_status tagpu_server_get_stats(tagpu_server* s, tagpu_server_stats* st) {
+  if (!s || !st) return TAGPU_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->m);
+  *st = tagpu_server_stats{};
+  st->submitted = s->submitted;
+  st->completed = s->completed;
+  st->rejected = s->rejected;
+  st->failed = s->failed;
+  st->batches = s->batches;
+  st->flops = s->flops;
+  st->wall_ms = s->t_first >= 0 ? s->t_last - s->t_first : 0;
+  st->bytes_in_use = s->in_use;
+  st->peak_bytes = s->peak;
+  if (!s->lat.empty()) {
+    std::vector<double> v = s->lat;
+    std::sort(v.begin(), v.end());
+    auto pct = [&](double p) {
+      const double x = p * (v.size() - 1);
+      const size_t i = (size_t)x;
+      const double f = x - i;
+      return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
+    };
+    st->p50_ms = pct(0.50);
+    st->p99_ms = pct(0.99);
+    double sum = 0;
+    for (double x : v) sum += x;
+    st->mean_ms = sum / v.size();
+  }
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_server_stop(tagpu_server* s) {
+  if (!s) return TAGPU_ERR_INVALID;
+  {
+    std::lock_guard<std::mutex> lk(s->m);
+    s->stopping = true;
+  }
+  s->cv.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  {
+    std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+    for (auto& kv : s->all)
+      if (kv.second->C) delete kv.second->C;
+    s->all.clear();
+  }
+  cudaStreamDestroy(s->gemm_stream);
+  delete s;
   return TAGPU_OK;
 }
 
