@@ -103,6 +103,16 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
                         OzakiPlan** out, std::string* err);
 void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s);
 void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s);
+// One launch over the output blocks of several plans with the same slice
+// count: d_params holds their parameter blocks (ozaki_params), d_vstart the
+// prefix sums of their block counts; d_err receives a wait timeout.
+void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int nviews,
+                              int64_t nblk, int slices, int* d_err, int sm_count,
+                              cudaStream_t s);
+size_t ozaki_params_size();
+void ozaki_params(const OzakiPlan* pl, void* out);
+int ozaki_slices(const OzakiPlan* pl);
+int* ozaki_error_flag(OzakiPlan* pl);
 int ozaki_error(OzakiPlan* pl);   // synchronises; 0 = ok
 size_t ozaki_scratch_bytes(const OzakiPlan* pl);
 int64_t ozaki_blocks(const OzakiPlan* pl);

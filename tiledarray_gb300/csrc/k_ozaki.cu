@@ -208,8 +208,22 @@ struct Smem {
   static constexpr int kBytes = kStages * kStageBytes + 1024;
 };
 
+// Output blocks of several contractions form one list: block gb belongs to
+// view v with vstart[v] <= gb < vstart[v+1].
+__device__ __forceinline__ int find_view(const int64_t* __restrict__ vstart, int nviews,
+                                         int64_t gb) {
+  int lo = 0, hi = nviews;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (vstart[mid] <= gb) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
 template <int S>
-__global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(OzParams P) {
+__global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
+    const OzParams* __restrict__ views, const int64_t* __restrict__ vstart, int nviews,
+    int64_t nblk_total, int* __restrict__ err) {
   constexpr int STAGES = Smem<S>::kStages;
   constexpr int STAGE_BYTES = Smem<S>::kStageBytes;
   constexpr int LEVELS = S + 1;
@@ -245,7 +259,7 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(OzParams P) {
 
   auto fail = [&](int code) {
     abort_s = 1;
-    atomicCAS(P.err, 0, code);
+    atomicCAS(err, 0, code);
   };
 
   if (warp == 0) {
@@ -257,7 +271,10 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(OzParams P) {
       bool issued[STAGES];
       for (int s = 0; s < STAGES; ++s) issued[s] = false;
       bool ok = true;
-      for (int64_t b = blockIdx.x; b < P.nblk && ok; b += gridDim.x) {
+      for (int64_t gb = blockIdx.x; gb < nblk_total && ok; gb += gridDim.x) {
+        const int vi = find_view(vstart, nviews, gb);
+        const OzParams& P = views[vi];
+        const int64_t b = gb - vstart[vi];
         const int rb = P.blk[2 * b], cb = P.blk[2 * b + 1];
         for (int64_t x = P.blk_off[b]; x < P.blk_off[b + 1]; ++x) {
           const int kb = P.blk_kb[x];
@@ -298,7 +315,10 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(OzParams P) {
     int stage = 0;
     uint32_t phase = 0, acc_phase = 0;
     bool ok = true;
-    for (int64_t b = blockIdx.x; b < P.nblk && ok; b += gridDim.x) {
+    for (int64_t gb = blockIdx.x; gb < nblk_total && ok; gb += gridDim.x) {
+      const int vi = find_view(vstart, nviews, gb);
+      const OzParams& P = views[vi];
+      const int64_t b = gb - vstart[vi];
       const int64_t n = P.blk_off[b + 1] - P.blk_off[b];
       for (int64_t x = 0; x < n && ok; ++x) {
         if (!mbar_wait(smem_u32(&bar_full[stage]), phase, &abort_s)) {
@@ -370,7 +390,10 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(OzParams P) {
       tmem_wait_st();
     }
     bool ok = true;
-    for (int64_t b = blockIdx.x; b < P.nblk && ok; b += gridDim.x) {
+    for (int64_t gb = blockIdx.x; gb < nblk_total && ok; gb += gridDim.x) {
+      const int vi = find_view(vstart, nviews, gb);
+      const OzParams& P = views[vi];
+      const int64_t b = gb - vstart[vi];
       const int rb = P.blk[2 * b], cb = P.blk[2 * b + 1];
       const int64_t n = P.blk_off[b + 1] - P.blk_off[b];
       const int64_t events = (n + NORM_STAGES - 1) / NORM_STAGES;
@@ -719,6 +742,8 @@ struct OzakiPlan {
   uint8_t *Apack = nullptr, *Bpack = nullptr;
   int* err = nullptr;
   OzParams P{};
+  OzParams* d_params = nullptr;   // P on the device (single-view launches)
+  int64_t* d_vstart = nullptr;    // {0, nblk}
   size_t bytes = 0;
   ~OzakiPlan() {
     for (auto& b : bufs)
@@ -751,7 +776,8 @@ struct OzakiPlan {
 namespace {
 
 template <int S>
-void launch_gemm_t(const OzakiPlan& pl, int sm_count, cudaStream_t st) {
+void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int64_t nblk,
+                   int* err, int sm_count, cudaStream_t st) {
   const size_t smem = Smem<S>::kBytes;
   static bool set = false;
   if (!set) {
@@ -759,8 +785,9 @@ void launch_gemm_t(const OzakiPlan& pl, int sm_count, cudaStream_t st) {
                          (int)smem);
     set = true;
   }
-  const int64_t grid = std::min<int64_t>(pl.nblk, sm_count);
-  if (grid > 0) ozaki_gemm_kernel<S><<<(unsigned)grid, THREADS, smem, st>>>(pl.P);
+  const int64_t grid = std::min<int64_t>(nblk, sm_count);
+  if (grid > 0)
+    ozaki_gemm_kernel<S><<<(unsigned)grid, THREADS, smem, st>>>(views, vstart, nviews, nblk, err);
 }
 
 template <int S>
@@ -974,6 +1001,12 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   P.M_total = pl->M_total;
   P.N_total = pl->N_total;
   P.err = pl->err;
+  if ((st = pl->alloc(&pl->d_params, 1, err)) || (st = pl->alloc(&pl->d_vstart, 2, err)))
+    return st;
+  const int64_t vs[2] = {0, pl->nblk};
+  cudaMemcpyAsync(pl->d_params, &P, sizeof(OzParams), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(pl->d_vstart, vs, sizeof(vs), cudaMemcpyHostToDevice, s);
+  cudaStreamSynchronize(s);
   *out = pl.release();
   return TAGPU_OK;
 }
@@ -999,16 +1032,28 @@ void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s) {
   }
 }
 
-void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s) {
-  switch (pl->S) {
-    case 2: launch_gemm_t<2>(*pl, sm_count, s); break;
-    case 3: launch_gemm_t<3>(*pl, sm_count, s); break;
-    case 4: launch_gemm_t<4>(*pl, sm_count, s); break;
-    case 5: launch_gemm_t<5>(*pl, sm_count, s); break;
-    case 6: launch_gemm_t<6>(*pl, sm_count, s); break;
-    default: launch_gemm_t<7>(*pl, sm_count, s); break;
+void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int nviews,
+                              int64_t nblk, int slices, int* d_err, int sm_count,
+                              cudaStream_t s) {
+  const OzParams* v = static_cast<const OzParams*>(d_params);
+  switch (slices) {
+    case 2: launch_gemm_t<2>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
+    case 3: launch_gemm_t<3>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
+    case 4: launch_gemm_t<4>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
+    case 5: launch_gemm_t<5>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
+    case 6: launch_gemm_t<6>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
+    default: launch_gemm_t<7>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
   }
 }
+
+void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s) {
+  ozaki_enqueue_gemm_views(pl->d_params, pl->d_vstart, 1, pl->nblk, pl->S, pl->err, sm_count, s);
+}
+
+size_t ozaki_params_size() { return sizeof(OzParams); }
+void ozaki_params(const OzakiPlan* pl, void* out) { *static_cast<OzParams*>(out) = pl->P; }
+int ozaki_slices(const OzakiPlan* pl) { return pl->S; }
+int* ozaki_error_flag(OzakiPlan* pl) { return pl->err; }
 
 int ozaki_error(OzakiPlan* pl) {
   int e = 0;

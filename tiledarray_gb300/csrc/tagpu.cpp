@@ -1258,11 +1258,27 @@ void move_into(tagpu_array* dst, tagpu_array* src) {
 
 namespace tagpu {
 
+// Device-side work lists of one launch set (kept alive while it may replay).
+struct LaunchBufs {
+  DBuf views, items;            // DMMA contraction views and 64x64 work items
+  DBuf ozp[8], ozv[8];          // emulated form: parameter blocks, block offsets
+  int64_t oz_nblk[8] = {0};
+  explicit LaunchBufs(tagpu_ctx* c) : views(c), items(c) {
+    for (int i = 0; i < 8; ++i) {
+      ozp[i].ctx = c;
+      ozv[i].ctx = c;
+    }
+  }
+};
+
 // Kernel (d) and the post-permutation for a set of planned contractions;
 // no host synchronisation, so the sequence can be captured in a graph.
-tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, DBuf& d_views,
-                           DBuf& d_items, bool upload, cudaStream_t stream = nullptr) {
+// upload: (re)build the device work lists first (outside any capture).
+tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, LaunchBufs& lb,
+                           bool upload, cudaStream_t stream = nullptr) {
   if (!stream) stream = ctx->stream;
+  DBuf& d_views = lb.views;
+  DBuf& d_items = lb.items;
   std::vector<GemmView> views;
   std::vector<WorkItem> items;
   for (auto* c : cs) {
@@ -1281,11 +1297,38 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, DBuf& 
     if ((e = upload_vec(ctx, d_views, views)) || (e = upload_vec(ctx, d_items, items))) return e;
     if (stream != ctx->stream) CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   }
+  // emulated form: frames and splitting per contraction, then one GEMM launch
+  // per slice count over the output blocks of all of them
+  std::vector<Contraction*> by_s[8];
   for (auto* c : cs) {
     if (!c->emulated()) continue;
     ozaki_enqueue(c->oz, ctx->sm_count, stream);
-    ozaki_enqueue_gemm(c->oz, ctx->sm_count, stream);
+    by_s[ozaki_slices(c->oz)].push_back(c);
     c->st.gemm_launches = 5;
+  }
+  for (int S = 2; S < 8; ++S) {
+    auto& g = by_s[S];
+    if (g.empty()) continue;
+    if (g.size() == 1) {
+      ozaki_enqueue_gemm(g[0]->oz, ctx->sm_count, stream);
+      continue;
+    }
+    if (upload) {
+      const size_t psz = ozaki_params_size();
+      std::vector<uint8_t> params(psz * g.size());
+      std::vector<int64_t> vstart(1, 0);
+      for (size_t i = 0; i < g.size(); ++i) {
+        ozaki_params(g[i]->oz, params.data() + i * psz);
+        vstart.push_back(vstart.back() + ozaki_blocks(g[i]->oz));
+      }
+      tagpu_status e;
+      if ((e = upload_vec(ctx, lb.ozp[S], params)) || (e = upload_vec(ctx, lb.ozv[S], vstart)))
+        return e;
+      lb.oz_nblk[S] = vstart.back();
+      if (stream != ctx->stream) CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    ozaki_enqueue_gemm_views(lb.ozp[S].p, lb.ozv[S].as<int64_t>(), (int)g.size(), lb.oz_nblk[S],
+                             S, ozaki_error_flag(g[0]->oz), ctx->sm_count, stream);
   }
   if (!items.empty()) {
     launch_dmma_gemm(stream, d_views.as<GemmView>(), d_items.as<WorkItem>(),
@@ -1310,7 +1353,7 @@ tagpu_status contract_impl(tagpu_ctx* ctx, const char* c_idx, double alpha, tagp
   Contraction c(ctx);
   tagpu_status e = plan_all(c, c_idx, alpha, A, a_idx, B, b_idx, opts);
   if (e) return e;
-  DBuf dv(ctx), di(ctx);
+  LaunchBufs lbuf(ctx);
   std::vector<Contraction*> cs{&c};
   if (c.emulated()) {
     EventTimer t_split(ctx->stream);
@@ -1331,7 +1374,7 @@ tagpu_status contract_impl(tagpu_ctx* ctx, const char* c_idx, double alpha, tagp
                   "emulated GEMM: a bounded wait ran out (role code %d); results invalid", oe);
   } else {
     EventTimer tm(ctx->stream);
-    if ((e = enqueue_gemms(ctx, cs, dv, di, true))) return e;
+    if ((e = enqueue_gemms(ctx, cs, lbuf, true))) return e;
     tm.stop();
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     c.st.ms_gemm = tm.ms();
@@ -1361,11 +1404,11 @@ struct tagpu_batch {
   };
   std::vector<Entry> entries;
   bool planned = false;
-  DBuf d_views, d_items;
+  LaunchBufs lb;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   tagpu_contract_stats stats{};
-  explicit tagpu_batch(tagpu_ctx* c) : ctx(c), d_views(c), d_items(c) {}
+  explicit tagpu_batch(tagpu_ctx* c) : ctx(c), lb(c) {}
   ~tagpu_batch() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -1437,13 +1480,13 @@ tagpu_status tagpu_batch_run(tagpu_batch* b) {
       fill_stats(c);
     }
     // run once eagerly (uploads the work lists), then capture the launches
-    if ((e = enqueue_gemms(ctx, cs, b->d_views, b->d_items, true))) return e;
+    if ((e = enqueue_gemms(ctx, cs, b->lb, true))) return e;
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     for (auto* c : cs)
       if (c->emulated() && ozaki_error(c->oz))
         return fail(ctx, TAGPU_ERR_TIMEOUT, "emulated GEMM: a bounded wait ran out");
     CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    e = enqueue_gemms(ctx, cs, b->d_views, b->d_items, false);
+    e = enqueue_gemms(ctx, cs, b->lb, false);
     cudaGraph_t g = nullptr;
     cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
     if (e) return e;
@@ -1719,7 +1762,7 @@ size_t footprint_bound(tagpu_array* A, const std::vector<std::string>& ai, tagpu
 
 void tagpu_server::run() {
   std::vector<std::shared_ptr<Req>> inflight;  // GEMMs enqueued on gemm_stream
-  DBuf dv_a(ctx), di_a(ctx), dv_b(ctx), di_b(ctx);
+  LaunchBufs lb_a(ctx), lb_b(ctx);
   bool use_a = true;
   auto finish_inflight = [&]() {
     if (inflight.empty()) return;
@@ -1802,10 +1845,9 @@ void tagpu_server::run() {
     if (!ok.empty()) {
       std::lock_guard<std::recursive_mutex> lk(ctx->mu);
       cudaSetDevice(ctx->device);
-      DBuf& dv = use_a ? dv_a : dv_b;
-      DBuf& di = use_a ? di_a : di_b;
+      LaunchBufs& lb = use_a ? lb_a : lb_b;
       use_a = !use_a;
-      tagpu_status e = enqueue_gemms(ctx, cs, dv, di, true, gemm_stream);
+      tagpu_status e = enqueue_gemms(ctx, cs, lb, true, gemm_stream);
       const uint64_t bid = next_batch++;
       for (auto& r : ok) {
         r->res.batch_size = (int)ok.size();
