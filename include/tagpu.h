@@ -149,7 +149,7 @@ tagpu_status tagpu_array_get_hashmarks(const tagpu_array* a, int d,
 /* ---- contraction -------------------------------------------------------- */
 typedef struct tagpu_contract_opts {
   int precision;              /* tagpu_precision */
-  int slices;                 /* Ozaki slices per operand, 0 = default (6) */
+  int slices;                 /* Ozaki slices per operand, 2..6, 0 = default (6) */
   float threshold;            /* result screening threshold, <0 = default */
 } tagpu_contract_opts;
 

@@ -67,7 +67,7 @@ def test_ozaki_uniform_vs_oracle(oracle, ta, world, n, lo, hi, seed, decay):
     assert st["pairs"] == stp["pairs"]
 
 
-@pytest.mark.parametrize("slices,bound", [(4, 1e-7), (5, 1e-9), (6, 1e-12), (7, 1e-12)])
+@pytest.mark.parametrize("slices,bound", [(3, 1e-5), (4, 1e-7), (5, 1e-9), (6, 1e-12)])
 def test_ozaki_slices(oracle, ta, world, slices, bound):
     h = uneven(400, 40, 120, 9)
     A, _ = gpu_operand(ta, world, [h, h], 5, 0, kind=0)
@@ -82,9 +82,10 @@ def test_ozaki_slices(oracle, ta, world, slices, bound):
     assert err <= bound
 
 
-def test_ozaki_carry_normalisation_exact(ta, world):
+def test_ozaki_long_k_exact(ta, world):
     """All-positive integer data over a long k: every level grows at the
-    worst-case rate, so the carries must keep the fp32 sums exact."""
+    worst-case rate within a chunk and the int64 drains must keep the whole
+    sum exact."""
     hk = uneven(6000, 100, 256, 11)
     hm = [0, 130, 257]
     A, _ = gpu_operand(ta, world, [hm, hk], 1, 0, kind=1)

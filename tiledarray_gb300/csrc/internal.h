@@ -12,6 +12,11 @@
 
 namespace tagpu {
 
+// Record a message as the context's last error and return `st`.
+tagpu_status set_last_error(tagpu_ctx* ctx, tagpu_status st, const char* msg);
+// Device ordinal of a context.
+int context_device(const tagpu_ctx* ctx);
+
 // ---------------------------------------------------------------------------
 // kernel launchers (defined in the .cu files); all asynchronous on `s`
 // ---------------------------------------------------------------------------

@@ -17,14 +17,19 @@
 //    in shared memory, so one bulk copy moves a brick into place;
 //  * products: for each pair (p, q) with p + q <= S + 1 one
 //    tcgen05.mma.kind::f16 (bf16 x bf16 -> fp32, M=128, N=64, K=16) adds
-//    D_p * E_q into the accumulator of level t = p + q in tensor memory.  All
-//    products are integers below 2^14 and every level is kept below 2^24 by
-//    a carry normalisation every 128 k (digits above 2^8 move one level up, the
-//    top level L1 only collects carries), so every fp32 sum is exact integer
-//    arithmetic;
-//  * recombination (the only FP64 arithmetic): at the end of an
-//    output block, C = alpha * 2^(E_A + E_B) * sum_t L_t 2^(2-8t), written into
-//    the result tiles the block overlaps.
+//    D_p * E_q into the tensor-memory accumulator of level t = p + q.  Every
+//    product is an integer below 2^14; each chunk of 128 k starts from fresh
+//    accumulators, so a level collects at most (t-1)*128 products and stays
+//    below 6*128*2^14 < 2^24: every fp32 sum is exact integer arithmetic;
+//  * draining: after a chunk the epilogue warps read each level (top level
+//    first, releasing it to the MMA warp at once through a per-level
+//    mbarrier, so the next chunk's MMAs overlap the drain) and fold it into
+//    two exact int64 accumulators per element, hi = L2*2^8 + L3 and
+//    lo = sum_{t>=4} L_t*2^(8(S+1-t));
+//  * recombination (the only FP64 arithmetic): at the end of an output block
+//    C = alpha * 2^(E_A + E_B) * (hi*2^-22 + lo*2^(2-8(S+1))), written into
+//    the result tiles the block overlaps, while the MMA warp already runs the
+//    next block.
 // Work is in global fused coordinates (output blocks 128 x 64, k blocks of
 // 32), so uneven tiles cost no padding except at block-sparsity boundaries;
 // a brick is stored only if some nonzero tile overlaps it, a k block is run
@@ -47,11 +52,11 @@ namespace {
 constexpr int BM = 128;            // output block rows (MMA M)
 constexpr int BN = 64;             // output block columns (MMA N)
 constexpr int BK = 32;             // k per stage (two MMA K = 16 steps)
-constexpr int NORM_STAGES = 4;     // carry normalisation every 128 k
+constexpr int CHUNK_STAGES = 4;    // fresh accumulators every 128 k (exact fp32 sums)
 constexpr int A_SLICE_BYTES = BM * BK * 2;   // 8 KB
 constexpr int B_SLICE_BYTES = BN * BK * 2;   // 4 KB
-constexpr int EPI_WARPS = 4;
-constexpr int THREADS = 64 + EPI_WARPS * 32; // producer, MMA, 4 epilogue warps
+constexpr int EPI_WARPS = 8;
+constexpr int THREADS = 64 + EPI_WARPS * 32; // producer, MMA, 8 epilogue warps
 constexpr unsigned long long WAIT_NS = 4000000000ull;  // 4 s bound per wait
 
 // ---------------------------------------------------------------------------
@@ -134,23 +139,8 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 #pragma unroll
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
-      "%13,%14,%15,%16};"
-      ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])),
-        "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])),
-        "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
-        "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])),
-        "r"(__float_as_uint(v[11])), "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])),
-        "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
-      : "memory");
-}
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_wait_st() {
-  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
 // K-major, no-swizzle operand image: core matrices of 8 rows x 16 bytes,
@@ -181,8 +171,8 @@ struct OzParams {
   const uint8_t* Bpack;      // B bricks, S * 4 KB each
   const int32_t* brickA;     // RB x KBn -> slot or -1
   const int32_t* brickB;     // KBn x CB -> slot or -1
-  const int32_t* blk;        // nblk x 2 (rb, cb)
-  const int64_t* blk_off;    // nblk + 1
+  const int32_t* blk;        // nblk x 2 (rb, cb), in scheduling order
+  const int64_t* blk_rng;    // nblk x 2: [begin, end) of the block's k blocks in blk_kb
   const int32_t* blk_kb;     // k blocks per output block
   int64_t nblk;
   int KBn, CB;
@@ -226,10 +216,10 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
     int64_t nblk_total, int* __restrict__ err) {
   constexpr int STAGES = Smem<S>::kStages;
   constexpr int STAGE_BYTES = Smem<S>::kStageBytes;
-  constexpr int LEVELS = S + 1;
+  constexpr int TOP = S + 1;         // highest level (levels 2..S+1 are MMA targets)
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES];
-  __shared__ __align__(8) uint64_t bar_acc_full, bar_acc_empty, bar_done;
+  __shared__ __align__(8) uint64_t bar_acc_full, bar_level[TOP + 1], bar_done;
   __shared__ uint32_t tmem_base_s;
   __shared__ volatile int abort_s;
 
@@ -242,7 +232,7 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
       mbar_init(smem_u32(&bar_empty[s]), 1);
     }
     mbar_init(smem_u32(&bar_acc_full), 1);
-    mbar_init(smem_u32(&bar_acc_empty), EPI_WARPS * 32);
+    for (int t = 0; t <= TOP; ++t) mbar_init(smem_u32(&bar_level[t]), EPI_WARPS * 32);
     mbar_init(smem_u32(&bar_done), 1);
     abort_s = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -256,6 +246,7 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base_s;
+  // level t (2..TOP) accumulates in tensor-memory columns [(t-2)*BN, (t-1)*BN)
 
   auto fail = [&](int code) {
     abort_s = 1;
@@ -276,7 +267,7 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
         const OzParams& P = views[vi];
         const int64_t b = gb - vstart[vi];
         const int rb = P.blk[2 * b], cb = P.blk[2 * b + 1];
-        for (int64_t x = P.blk_off[b]; x < P.blk_off[b + 1]; ++x) {
+        for (int64_t x = P.blk_rng[2 * b]; x < P.blk_rng[2 * b + 1]; ++x) {
           const int kb = P.blk_kb[x];
           if (!mbar_wait(smem_u32(&bar_empty[stage]), phase ^ 1, &abort_s)) {
             fail(1);
@@ -303,7 +294,6 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
       // copies still in flight land before the CTA may exit
       for (int s = 0; s < STAGES; ++s)
         if (issued[s] && !mbar_wait(smem_u32(&bar_full[s]), issued_parity[s], &abort_s)) {
-          // the abort flag may be set: wait once more without it
           const uint64_t t0 = globaltimer();
           while (!mbar_try(smem_u32(&bar_full[s]), issued_parity[s]) &&
                  globaltimer() - t0 < WAIT_NS) {
@@ -312,57 +302,67 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
     }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
+    // Chunks of CHUNK_STAGES stages start from fresh accumulators; before the
+    // first MMA of a chunk into level t, the epilogue must have drained level
+    // t of the previous chunk.  Levels are issued from the top down, the order
+    // in which the epilogue drains them.
     int stage = 0;
-    uint32_t phase = 0, acc_phase = 0;
+    uint32_t phase = 0;
+    int64_t chunk = 0;   // chunks issued by this CTA
     bool ok = true;
     for (int64_t gb = blockIdx.x; gb < nblk_total && ok; gb += gridDim.x) {
       const int vi = find_view(vstart, nviews, gb);
       const OzParams& P = views[vi];
       const int64_t b = gb - vstart[vi];
-      const int64_t n = P.blk_off[b + 1] - P.blk_off[b];
+      const int64_t n = P.blk_rng[2 * b + 1] - P.blk_rng[2 * b];
       for (int64_t x = 0; x < n && ok; ++x) {
+        const bool chunk_start = (x % CHUNK_STAGES) == 0;
+        const bool chunk_end = ((x + 1) % CHUNK_STAGES) == 0 || x == n - 1;
         if (!mbar_wait(smem_u32(&bar_full[stage]), phase, &abort_s)) {
           fail(2);
           ok = false;
           break;
         }
         tc_fence_after();
-        if (lane == 0) {
-          const uint32_t sbase = smem_u32(stage_base + stage * STAGE_BYTES);
-          const bool fresh = (x == 0);
+        const uint32_t sbase = smem_u32(stage_base + stage * STAGE_BYTES);
 #pragma unroll
-          for (int ks = 0; ks < 2; ++ks) {
+        for (int t = TOP; t >= 2; --t) {
+          if (chunk_start && chunk > 0) {
+            if (!mbar_wait(smem_u32(&bar_level[t]), (uint32_t)((chunk - 1) & 1), &abort_s)) {
+              fail(3);
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+          }
+          if (lane == 0) {
 #pragma unroll
-            for (int t = 2; t <= S + 1; ++t) {
+            for (int ks = 0; ks < 2; ++ks) {
 #pragma unroll
               for (int p = 1; p < t; ++p) {
                 const int q = t - p;
                 if (p > S || q > S) continue;
                 const uint32_t a = sbase + (p - 1) * A_SLICE_BYTES + ks * 256;
-                const uint32_t bb = sbase + S * A_SLICE_BYTES + (q - 1) * B_SLICE_BYTES + ks * 256;
-                const uint32_t acc = (fresh && ks == 0 && p == 1) ? 0u : 1u;
-                tc_mma(tmem + (t - 1) * BN, make_desc(a), make_desc(bb), kIdesc, acc);
+                const uint32_t bb =
+                    sbase + S * A_SLICE_BYTES + (q - 1) * B_SLICE_BYTES + ks * 256;
+                const uint32_t acc = (chunk_start && ks == 0 && p == 1) ? 0u : 1u;
+                tc_mma(tmem + (t - 2) * BN, make_desc(a), make_desc(bb), kIdesc, acc);
               }
             }
           }
-          tc_commit(smem_u32(&bar_empty[stage]));
+          __syncwarp();
         }
+        if (!ok) break;
+        if (lane == 0) tc_commit(smem_u32(&bar_empty[stage]));
         __syncwarp();
         if (++stage == STAGES) {
           stage = 0;
           phase ^= 1;
         }
-        const bool last = (x == n - 1);
-        if (last || ((x + 1) % NORM_STAGES) == 0) {
+        if (chunk_end) {
           if (lane == 0) tc_commit(smem_u32(&bar_acc_full));
           __syncwarp();
-          if (!mbar_wait(smem_u32(&bar_acc_empty), acc_phase, &abort_s)) {
-            fail(3);
-            ok = false;
-            break;
-          }
-          acc_phase ^= 1;
-          tc_fence_after();
+          ++chunk;
         }
       }
     }
@@ -376,106 +376,81 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
     }
   } else {
     // ------------------------------------------------------------ epilogue
+    // Eight warps: warp % 4 selects the 32 tensor-memory lanes (rows) a warp
+    // may access, (warp - 2) / 4 the half of the 64 columns it owns.  Each
+    // chunk's levels are read, released, and folded into two exact int64
+    // accumulators per element: hi = L2*2^8 + L3 (unit of level 3) and
+    // lo = sum_{t>=4} L_t*2^(8(TOP-t)) (unit of level TOP).
     const int quarter = warp & 3;
+    const int half = (warp - 2) >> 2;
     const int rloc = quarter * 32 + lane;
-    const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
-    uint32_t acc_phase = 0;
-    {
-      // L1 only collects carries: start from zero
-      float z[16];
-#pragma unroll
-      for (int i = 0; i < 16; ++i) z[i] = 0.0f;
-#pragma unroll
-      for (int c = 0; c < BN; c += 16) tmem_st16(lane_addr + c, z);
-      tmem_wait_st();
-    }
+    const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16) + half * 32;
+    int64_t chunk = 0;
     bool ok = true;
+    int64_t hi[32], lo[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) hi[j] = lo[j] = 0;
     for (int64_t gb = blockIdx.x; gb < nblk_total && ok; gb += gridDim.x) {
       const int vi = find_view(vstart, nviews, gb);
       const OzParams& P = views[vi];
       const int64_t b = gb - vstart[vi];
       const int rb = P.blk[2 * b], cb = P.blk[2 * b + 1];
-      const int64_t n = P.blk_off[b + 1] - P.blk_off[b];
-      const int64_t events = (n + NORM_STAGES - 1) / NORM_STAGES;
-      for (int64_t ev = 0; ev < events; ++ev) {
-        if (!mbar_wait(smem_u32(&bar_acc_full), acc_phase, &abort_s)) {
+      const int64_t n = P.blk_rng[2 * b + 1] - P.blk_rng[2 * b];
+      const int64_t nchunks = (n + CHUNK_STAGES - 1) / CHUNK_STAGES;
+      for (int64_t c = 0; c < nchunks; ++c, ++chunk) {
+        if (!mbar_wait(smem_u32(&bar_acc_full), (uint32_t)(chunk & 1), &abort_s)) {
           fail(4);
           ok = false;
           break;
         }
-        acc_phase ^= 1;
         tc_fence_after();
-        const bool final_ev = (ev == events - 1);
-        if (!final_ev) {
-          // carry normalisation: every level back to |L_t| <= 128 (t >= 2)
-#pragma unroll 1
-          for (int c = 0; c < BN; c += 16) {
-            float L[LEVELS][16];
 #pragma unroll
-            for (int t = 0; t < LEVELS; ++t) tmem_ld16(lane_addr + t * BN + c, L[t]);
-            tmem_wait_ld();
+        for (int t = TOP; t >= 2; --t) {
+          float v0[16], v1[16];
+          tmem_ld16(lane_addr + (t - 2) * BN, v0);
+          tmem_ld16(lane_addr + (t - 2) * BN + 16, v1);
+          tmem_wait_ld();
+          tc_fence_before();
+          mbar_arrive(smem_u32(&bar_level[t]));
+          if (t >= 4) {
+            const int sh = 8 * (TOP - t);
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-              float carry = 0.0f;
-#pragma unroll
-              for (int t = LEVELS - 1; t >= 1; --t) {
-                const float xv = L[t][j] + carry;
-                const float h = rintf(xv * 0.00390625f);
-                L[t][j] = fmaf(-256.0f, h, xv);
-                carry = h;
-              }
-              L[0][j] += carry;
+              lo[j] += (int64_t)__float2int_rn(v0[j]) << sh;
+              lo[16 + j] += (int64_t)__float2int_rn(v1[j]) << sh;
             }
+          } else {
+            const int sh = 8 * (3 - t);
 #pragma unroll
-            for (int t = 0; t < LEVELS; ++t) tmem_st16(lane_addr + t * BN + c, L[t]);
-            tmem_wait_st();
-          }
-        } else {
-          // recombination and store into the result tiles
-          const int64_t gr = (int64_t)rb * BM + rloc;
-          const bool row_ok = gr < P.M_total;
-          int ti = 0, lr = 0, ea = 0;
-          if (row_ok) {
-            ti = P.row_tile[gr];
-            lr = P.row_local[gr];
-            ea = P.EA[gr];
-          }
-#pragma unroll 1
-          for (int c = 0; c < BN; c += 16) {
-            float L[LEVELS][16];
-#pragma unroll
-            for (int t = 0; t < LEVELS; ++t) tmem_ld16(lane_addr + t * BN + c, L[t]);
-            tmem_wait_ld();
-            if (row_ok) {
-#pragma unroll
-              for (int j = 0; j < 16; ++j) {
-                const int64_t gc = (int64_t)cb * BN + c + j;
-                if (gc < P.N_total) {
-                  const int tj = P.col_tile[gc];
-                  const int64_t off = P.coff[(int64_t)ti * P.Nt + tj];
-                  if (off >= 0) {
-                    double v = 0.0;
-#pragma unroll
-                    for (int t = LEVELS - 1; t >= 0; --t)
-                      v = fma((double)L[t][j], level_unit(t + 1), v);
-                    const double val = P.alpha * ldexp(v, (ea - 1022) + (P.EB[gc] - 1022));
-                    P.C[off + (int64_t)lr * P.nsz[tj] + P.col_local[gc]] = val;
-                  }
-                }
-              }
+            for (int j = 0; j < 16; ++j) {
+              hi[j] += (int64_t)__float2int_rn(v0[j]) << sh;
+              hi[16 + j] += (int64_t)__float2int_rn(v1[j]) << sh;
             }
           }
-          // zero L1 for the next block
-          float z[16];
-#pragma unroll
-          for (int i = 0; i < 16; ++i) z[i] = 0.0f;
-#pragma unroll
-          for (int c = 0; c < BN; c += 16) tmem_st16(lane_addr + c, z);
-          tmem_wait_st();
         }
-        tc_fence_before();
-        mbar_arrive(smem_u32(&bar_acc_empty));
       }
+      if (!ok) break;
+      // recombination: C = alpha * 2^(E_A + E_B) * (hi * u3 + lo * u_TOP)
+      const int64_t gr = (int64_t)rb * BM + rloc;
+      if (gr < P.M_total) {
+        const int ti = P.row_tile[gr], lr = P.row_local[gr], ea = P.EA[gr];
+        const double u3 = level_unit(3), ut = level_unit(TOP);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int64_t gc = (int64_t)cb * BN + half * 32 + j;
+          if (gc < P.N_total) {
+            const int tj = P.col_tile[gc];
+            const int64_t off = P.coff[(int64_t)ti * P.Nt + tj];
+            if (off >= 0) {
+              const double v = fma((double)hi[j], u3, (double)lo[j] * ut);
+              P.C[off + (int64_t)lr * P.nsz[tj] + P.col_local[gc]] =
+                  P.alpha * ldexp(v, (ea - 1022) + (P.EB[gc] - 1022));
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 32; ++j) hi[j] = lo[j] = 0;
     }
   }
   tc_fence_before();
@@ -737,7 +712,7 @@ struct OzakiPlan {
           *col_tile = nullptr, *col_local = nullptr, *rstart = nullptr, *cstart = nullptr;
   int32_t *EA = nullptr, *EB = nullptr, *brickA = nullptr, *brickB = nullptr, *listA = nullptr,
           *listB = nullptr, *blk = nullptr, *blk_kb = nullptr;
-  int64_t *blk_off = nullptr, *workA = nullptr, *workB = nullptr;
+  int64_t *blk_off = nullptr, *blk_rng = nullptr, *workA = nullptr, *workB = nullptr;
   int64_t nworkA = 0, nworkB = 0;
   uint8_t *Apack = nullptr, *Bpack = nullptr;
   int* err = nullptr;
@@ -833,8 +808,8 @@ void index_maps(const int32_t* sz, int64_t n, std::vector<int32_t>& tile,
 tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
                         const int32_t* h_nsz, const int32_t* h_ksz, int slices,
                         OzakiPlan** out, std::string* err) {
-  if (slices < 2 || slices > 7) {
-    *err = "emulated form supports 2..7 slices";
+  if (slices < 2 || slices > 6) {
+    *err = "emulated form supports 2..6 slices";
     return TAGPU_ERR_INVALID;
   }
   auto pl = std::make_unique<OzakiPlan>();
@@ -966,6 +941,38 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   block_list_kernel<<<blocks_for(nob, 256), 256, 0, s>>>(counts, scan_b, nob, pl->CB, pl->blk);
   gather_offsets_kernel<<<blocks_for(nob, 256), 256, 0, s>>>(counts, scan_c, scan_b, nob,
                                                              pl->blk_off);
+  // Scheduling order: super-tiles of 8 row blocks x 19 column blocks (one
+  // wave of 152 CTAs), so CTAs running together share A bricks (19 ways) and
+  // B bricks (8 ways) in L2.
+  {
+    std::vector<int32_t> hb(2 * pl->nblk);
+    std::vector<int64_t> ho(pl->nblk + 1);
+    if (pl->nblk) {
+      cudaMemcpyAsync(hb.data(), pl->blk, hb.size() * 4, cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(ho.data(), pl->blk_off, ho.size() * 8, cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+    }
+    const int64_t GR = 8, GC = 19;
+    const int64_t nsc = (pl->CB + GC - 1) / GC;
+    std::vector<std::pair<int64_t, int64_t>> key(pl->nblk);
+    for (int64_t b = 0; b < pl->nblk; ++b) {
+      const int64_t rb = hb[2 * b], cb = hb[2 * b + 1];
+      const int64_t tile = (rb / GR) * nsc + cb / GC;
+      key[b] = {tile * GR * GC + (cb % GC) * GR + (rb % GR), b};
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<int32_t> nb(2 * pl->nblk);
+    std::vector<int64_t> rng(2 * pl->nblk);
+    for (int64_t i = 0; i < pl->nblk; ++i) {
+      const int64_t b = key[i].second;
+      nb[2 * i] = hb[2 * b];
+      nb[2 * i + 1] = hb[2 * b + 1];
+      rng[2 * i] = ho[b];
+      rng[2 * i + 1] = ho[b + 1];
+    }
+    if ((st = pl->upload(&pl->blk_rng, rng, err))) return st;
+    if (pl->nblk) cudaMemcpyAsync(pl->blk, nb.data(), nb.size() * 4, cudaMemcpyHostToDevice, s);
+  }
   // operand slices
   const size_t a_brick = (size_t)slices * A_SLICE_BYTES, b_brick = (size_t)slices * B_SLICE_BYTES;
   if ((st = pl->alloc(&pl->Apack, a_brick * pl->nA, err)) ||
@@ -982,7 +989,7 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   P.brickA = pl->brickA;
   P.brickB = pl->brickB;
   P.blk = pl->blk;
-  P.blk_off = pl->blk_off;
+  P.blk_rng = pl->blk_rng;
   P.blk_kb = pl->blk_kb;
   P.nblk = pl->nblk;
   P.KBn = (int)pl->KB;
@@ -1027,8 +1034,7 @@ void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s) {
     case 3: launch_split_t<3>(*pl, sm_count, s); break;
     case 4: launch_split_t<4>(*pl, sm_count, s); break;
     case 5: launch_split_t<5>(*pl, sm_count, s); break;
-    case 6: launch_split_t<6>(*pl, sm_count, s); break;
-    default: launch_split_t<7>(*pl, sm_count, s); break;
+    default: launch_split_t<6>(*pl, sm_count, s); break;
   }
 }
 
@@ -1041,8 +1047,7 @@ void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int
     case 3: launch_gemm_t<3>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
     case 4: launch_gemm_t<4>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
     case 5: launch_gemm_t<5>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
-    case 6: launch_gemm_t<6>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
-    default: launch_gemm_t<7>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
+    default: launch_gemm_t<6>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
   }
 }
 

@@ -140,6 +140,14 @@ tagpu_array::~tagpu_array() {
   if (data) dev_free(ctx, data, bytes);
 }
 
+namespace tagpu {
+tagpu_status set_last_error(tagpu_ctx* ctx, tagpu_status st, const char* msg) {
+  if (ctx) ctx->err = msg;
+  return st;
+}
+int context_device(const tagpu_ctx* ctx) { return ctx ? ctx->device : -1; }
+}  // namespace tagpu
+
 namespace {
 
 // Scoped device buffer on the context stream.
@@ -654,15 +662,16 @@ tagpu_status tagpu_array_generate(tagpu_array* a, uint64_t seed, uint64_t stream
   cudaSetDevice(ctx->device);
   if (kind != 0 && kind != 1) return fail(ctx, TAGPU_ERR_INVALID, "generate: kind must be 0 or 1");
   const int64_t n = a->ntiles();
-  // tiles present: scale != 0 (and, without compute_shape, nonzero in the shape)
+  // tiles generated: with compute_shape those with a nonzero scale (the shape
+  // follows from their norms); without it, every tile the current shape keeps
+  // (a zero scale then gives a zero tile)
   std::vector<int64_t> lo, offs(1, 0), present;
   std::vector<int32_t> ext;
   std::vector<double> scale;
   int64_t idx[8];
   for (int64_t t = 0; t < n; ++t) {
     const double sc = tile_scale ? tile_scale[t] : 1.0;
-    if (sc == 0.0) continue;
-    if (!compute_shape && a->tile_is_zero(t)) continue;
+    if (compute_shape ? sc == 0.0 : a->tile_is_zero(t)) continue;
     a->tile_index(t, idx);
     for (int d = 0; d < a->rank; ++d) {
       lo.push_back(a->hm[d][idx[d]] - a->hm[d][0]);
@@ -673,26 +682,38 @@ tagpu_status tagpu_array_generate(tagpu_array* a, uint64_t seed, uint64_t stream
     offs.push_back(offs.back() + a->tile_volume(t));
   }
   const int64_t np = (int64_t)present.size();
-  // generate into a temporary packed buffer over the present tiles
-  DBuf dlo(ctx), dext(ctx), doff(ctx), dsc(ctx), dtmp(ctx);
+  // Generate straight into the array's storage laid out over the present
+  // tiles (tile ordinal order), so peak memory is the array itself.
+  DBuf dlo(ctx), dext(ctx), doff(ctx), dsc(ctx);
   tagpu_status st;
   if ((st = upload_vec(ctx, dlo, lo)) || (st = upload_vec(ctx, dext, ext)) ||
       (st = upload_vec(ctx, doff, offs)) || (st = upload_vec(ctx, dsc, scale)))
     return st;
-  if ((st = dtmp.alloc(std::max<int64_t>(1, offs.back()) * sizeof(double)))) return st;
+  const size_t need = (size_t)offs.back() * sizeof(double);
+  if (a->bytes != need) {
+    if (a->data) dev_free(ctx, a->data, a->bytes);
+    a->data = nullptr;
+    a->bytes = 0;
+    if (need) {
+      void* p = nullptr;
+      if ((st = dev_alloc(ctx, &p, need))) return st;
+      a->data = static_cast<double*>(p);
+      a->bytes = need;
+    }
+  }
   GenDesc g{};
   g.rank = a->rank;
   for (int d = 0; d < a->rank; ++d) g.gext[d] = a->hm[d].back() - a->hm[d][0];
   g.seed = seed;
   g.stream = stream;
   g.kind = kind;
-  launch_generate(ctx->stream, g, np, dlo.as<int64_t>(), dext.as<int32_t>(),
-                  doff.as<int64_t>(), dsc.as<double>(), dtmp.as<double>());
+  launch_generate(ctx->stream, g, np, dlo.as<int64_t>(), dext.as<int32_t>(), doff.as<int64_t>(),
+                  dsc.as<double>(), a->data);
   CUDA_TRY(ctx, cudaGetLastError());
   if (compute_shape) {
     DBuf dn(ctx);
     if ((st = dn.alloc(std::max<int64_t>(1, np) * sizeof(float)))) return st;
-    launch_tile_norms(ctx->stream, np, doff.as<int64_t>(), dtmp.as<double>(), dn.as<float>());
+    launch_tile_norms(ctx->stream, np, doff.as<int64_t>(), a->data, dn.as<float>());
     CUDA_TRY(ctx, cudaGetLastError());
     std::vector<float> pn(np);
     if (np)
@@ -707,27 +728,50 @@ tagpu_status tagpu_array_generate(tagpu_array* a, uint64_t seed, uint64_t stream
     a->norms = norms;
     a->zero_count = scale_norms(a, a->norms, thr);
   }
-  pack_offsets(a);
-  if ((st = ensure_storage(a))) return st;
-  // move the present, nonzero tiles into place (contiguous runs when packed)
+  pack_offsets(a);  // offsets of the tiles that survived the shape
+  // Compact in place: surviving tiles move to lower addresses in ordinal
+  // order.  A tile whose source and destination overlap goes through a
+  // bounce buffer of one tile; disjoint runs are single copies.
+  DBuf bounce(ctx);
   int64_t x = 0;
   while (x < np) {
     const int64_t t = present[x];
-    if (a->off[t] < 0) {
+    const int64_t dst = a->off[t];
+    if (dst < 0 || dst == offs[x]) {
       ++x;
       continue;
     }
-    int64_t y = x + 1;
-    while (y < np && a->off[present[y]] >= 0 &&
-           a->off[present[y]] == a->off[present[y - 1]] + (offs[y] - offs[y - 1]) &&
-           true)
-      ++y;
-    CUDA_TRY(ctx, cudaMemcpyAsync(a->data + a->off[t], dtmp.as<double>() + offs[x],
-                                  (offs[y] - offs[x]) * sizeof(double), cudaMemcpyDeviceToDevice,
-                                  ctx->stream));
-    x = y;
+    const int64_t len = offs[x + 1] - offs[x];
+    if (dst + len <= offs[x]) {
+      CUDA_TRY(ctx, cudaMemcpyAsync(a->data + dst, a->data + offs[x], len * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, ctx->stream));
+    } else {
+      if (bounce.n < (size_t)len * sizeof(double) && (st = bounce.alloc(len * sizeof(double))))
+        return st;
+      CUDA_TRY(ctx, cudaMemcpyAsync(bounce.p, a->data + offs[x], len * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, ctx->stream));
+      CUDA_TRY(ctx, cudaMemcpyAsync(a->data + dst, bounce.p, len * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    ++x;
   }
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  // release the tail the dropped tiles occupied
+  const size_t keep = (size_t)a->elements * sizeof(double);
+  if (keep < a->bytes) {
+    void* p = nullptr;
+    if (keep && (st = dev_alloc(ctx, &p, keep)) == TAGPU_OK) {
+      CUDA_TRY(ctx, cudaMemcpyAsync(p, a->data, keep, cudaMemcpyDeviceToDevice, ctx->stream));
+      dev_free(ctx, a->data, a->bytes);
+      a->data = static_cast<double*>(p);
+      a->bytes = keep;
+    } else if (!keep) {
+      dev_free(ctx, a->data, a->bytes);
+      a->data = nullptr;
+      a->bytes = 0;
+    }
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  }
   return TAGPU_OK;
 }
 
@@ -1192,8 +1236,8 @@ tagpu_status plan_all(Contraction& c, const char* c_idx, double alpha, tagpu_arr
   const float cthr = opts && opts->threshold >= 0 ? opts->threshold : ctx->threshold;
   if (c.precision != TAGPU_PRECISION_FP64 && c.precision != TAGPU_PRECISION_OZAKI)
     return fail(ctx, TAGPU_ERR_INVALID, "unknown precision %d", c.precision);
-  if (c.precision == TAGPU_PRECISION_OZAKI && (c.slices < 2 || c.slices > 8))
-    return fail(ctx, TAGPU_ERR_INVALID, "slices must be 2..8");
+  if (c.precision == TAGPU_PRECISION_OZAKI && (c.slices < 2 || c.slices > 6))
+    return fail(ctx, TAGPU_ERR_INVALID, "slices must be 2..6");
   tagpu_status e;
   if ((e = plan_contraction(c, c_idx, alpha, A, a_idx, B, b_idx, cthr))) return e;
   if ((e = run_shape_and_pairs(c))) return e;
