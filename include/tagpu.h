@@ -197,6 +197,23 @@ tagpu_status tagpu_pair_list(tagpu_ctx* ctx, int64_t M, int64_t N, int64_t K,
                              const float* lnorm, float l_thr,
                              const float* rnorm, float r_thr, int64_t* offsets,
                              int32_t* kidx, int64_t kidx_cap, int64_t* npairs);
+/* Kernel (b) without any device allocation.  No counterpart in the
+ * reference: it serves callers that cannot allocate device memory (a host
+ * application whose device memory is owned by another framework's pool, or a
+ * latency-critical loop that must not allocate).  Every pointer is a device
+ * pointer supplied by the caller (offsets: M*N+1 entries; kidx: kidx_cap
+ * entries or NULL to count only); *npairs is written on the host.  The only
+ * scratch is a fixed per-device array of 2^20 result-tile counts inside the
+ * library, so M*N above 1,048,576 is rejected (TAGPU_ERR_INVALID).  The first
+ * call on a device looks the array up (make it before any stream capture);
+ * calls whose work overlaps on the GPU share the array and race.  stream:
+ * a cudaStream_t, NULL for the legacy default stream. */
+tagpu_status tagpu_pair_list_noalloc(tagpu_ctx* ctx, int64_t M, int64_t N, int64_t K,
+                                     const float* cnorm, float c_thr,
+                                     const float* lnorm, float l_thr,
+                                     const float* rnorm, float r_thr,
+                                     int64_t* offsets, int32_t* kidx, int64_t kidx_cap,
+                                     int64_t* npairs, void* stream);
 /* Kernel (c): out = permute(in, perm), result dim perm[d] = arg dim d. */
 tagpu_status tagpu_permute(tagpu_ctx* ctx, int rank, const int64_t* extents,
                            const int32_t* perm, const double* in, double* out);

@@ -146,6 +146,10 @@ SIGNATURES = {
                                        _f32p, ctypes.c_float, _f32p, ctypes.c_float, _f32p,
                                        ctypes.c_float, _i64p, _i32p, ctypes.c_int64, _i64p]),
     "tagpu_permute": (ctypes.c_int, [_vp, ctypes.c_int, _i64p, _i32p, _f64p, _f64p]),
+    "tagpu_pair_list_noalloc": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64,
+                                               ctypes.c_int64, _vp, ctypes.c_float, _vp,
+                                               ctypes.c_float, _vp, ctypes.c_float, _vp, _vp,
+                                               ctypes.c_int64, _i64p, _vp]),
     "tagpu_batch_create": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "tagpu_batch_add": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, _vp,
                                        ctypes.c_char_p, _vp, ctypes.c_char_p,
