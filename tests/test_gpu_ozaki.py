@@ -138,3 +138,15 @@ def test_ozaki_batch_graph(ta, world):
     for o, f in zip(outs, first):
         assert np.array_equal(o.download(), f)
     world.check(L.tagpu_batch_destroy(bh))
+
+
+def test_ozaki_row_chunking_identical(ta, world, monkeypatch):
+    """A digit bricks built and consumed one range of row blocks at a time
+    (forced by a tiny budget) give bit-identical results."""
+    h = uneven(1100, 48, 256, 21)
+    A, _ = gpu_operand(ta, world, [h, h], 4, 0, kind=0)
+    B, _ = gpu_operand(ta, world, [h, h], 4, 1, kind=0)
+    ref, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI)
+    monkeypatch.setenv("TAGPU_OZAKI_A_BYTES", str(3 * 6 * 8192 * 40))
+    got, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI)
+    assert np.array_equal(got.download(), ref.download())

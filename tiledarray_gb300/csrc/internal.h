@@ -114,6 +114,9 @@ void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s);
 void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int nviews,
                               int64_t nblk, int slices, int* d_err, int sm_count,
                               cudaStream_t s);
+// Number of row chunks (1 unless the A digit bricks would not fit at once;
+// chunked plans are launched on their own, not grouped with others).
+int ozaki_chunks(const OzakiPlan* pl);
 size_t ozaki_params_size();
 void ozaki_params(const OzakiPlan* pl, void* out);
 int ozaki_slices(const OzakiPlan* pl);

@@ -40,6 +40,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <memory>
 #include <string>
 #include <vector>
@@ -161,6 +162,61 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                             ((uint32_t)(BM >> 4) << 24);
 
+// Correctly rounded double of (hi * 2^sh + lo) * 2^e2 from exact integers
+// (|hi| < 2^61, |lo| < 2^62, 0 <= sh < 64), with integer instructions only;
+// FP64 arithmetic on this GPU is far slower than integer arithmetic.  The
+// rare results outside the normal range take the FP64 library route.
+__device__ __forceinline__ double exact_to_double(int64_t hi, int64_t lo, int sh, int e2) {
+  // 128-bit two's complement W = hi * 2^sh + lo
+  uint64_t wl = (uint64_t)hi << sh;
+  int64_t wh = sh ? (hi >> (64 - sh)) : (hi < 0 ? -1 : 0);
+  const uint64_t lo_u = (uint64_t)lo;
+  const uint64_t sum = wl + lo_u;
+  wh += (int64_t)(lo < 0 ? -1 : 0) + (sum < wl ? 1 : 0);
+  wl = sum;
+  const bool neg = wh < 0;
+  uint64_t mh = (uint64_t)wh, ml = wl;
+  if (neg) {  // magnitude
+    ml = ~ml + 1;
+    mh = ~mh + (ml == 0 ? 1 : 0);
+  }
+  if (mh == 0 && ml == 0) return 0.0;
+  const int lz = mh ? __clzll((long long)mh) : 64 + __clzll((long long)ml);
+  const int p = 127 - lz;                // position of the leading one
+  uint64_t mant;
+  if (p <= 52) {
+    mant = ml << (52 - p);
+  } else {
+    const int r = p - 52;                // bits dropped
+    // mantissa = W >> r, remainder bits for rounding
+    uint64_t q, rem_hi_bit, sticky;
+    if (r < 64) {
+      q = (ml >> r) | (r ? (mh << (64 - r)) : 0);
+      rem_hi_bit = (ml >> (r - 1)) & 1;
+      sticky = (r >= 2) ? (ml & ((1ull << (r - 1)) - 1)) : 0;
+    } else {
+      const int r2 = r - 64;
+      q = mh >> r2;
+      rem_hi_bit = r2 ? ((mh >> (r2 - 1)) & 1) : (ml >> 63);
+      sticky = (r2 >= 2 ? (mh & ((1ull << (r2 - 1)) - 1)) : 0) |
+               (r2 ? ml : (ml & ((1ull << 63) - 1)));
+    }
+    mant = q;
+    if (rem_hi_bit && (sticky || (mant & 1))) ++mant;
+  }
+  int ex = p + e2;                       // value = mant * 2^(ex - 52)
+  if (mant >> 53) {                      // rounding carried into a new bit
+    mant >>= 1;
+    ++ex;
+  }
+  if (ex < -1022 || ex > 1023) {
+    const double v = ldexp((double)(int64_t)mant, ex - 52);
+    return neg ? -v : v;
+  }
+  const uint64_t bits = ((uint64_t)(ex + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)(bits | (neg ? (1ull << 63) : 0)));
+}
+
 // 2^(2 - 8t): the unit of level t (products of digits d_p e_q with p + q = t)
 __device__ __forceinline__ double level_unit(int t) {
   return __longlong_as_double((long long)(1023 + 2 - 8 * t) << 52);
@@ -168,12 +224,13 @@ __device__ __forceinline__ double level_unit(int t) {
 
 struct OzParams {
   const uint8_t* Apack;      // A bricks, S * 8 KB each
+  int64_t a_slot_base;       // first A brick slot held in Apack (row chunking)
   const uint8_t* Bpack;      // B bricks, S * 4 KB each
   const int32_t* brickA;     // RB x KBn -> slot or -1
   const int32_t* brickB;     // KBn x CB -> slot or -1
   const int32_t* blk;        // nblk x 2 (rb, cb), in scheduling order
   const int64_t* blk_rng;    // nblk x 2: [begin, end) of the block's k blocks in blk_kb
-  const int32_t* blk_kb;     // k blocks per output block
+  const int2* blk_ab;        // per k block of a block: (A brick slot, B brick slot)
   int64_t nblk;
   int KBn, CB;
   const int32_t* EA;         // M_total frames (biased exponent; E = EA - 1022)
@@ -255,43 +312,54 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
-    if (lane == 0) {
-      int stage = 0;
-      uint32_t phase = 0;
-      uint32_t issued_parity[STAGES];
-      bool issued[STAGES];
-      for (int s = 0; s < STAGES; ++s) issued[s] = false;
-      bool ok = true;
-      for (int64_t gb = blockIdx.x; gb < nblk_total && ok; gb += gridDim.x) {
-        const int vi = find_view(vstart, nviews, gb);
-        const OzParams& P = views[vi];
-        const int64_t b = gb - vstart[vi];
-        const int rb = P.blk[2 * b], cb = P.blk[2 * b + 1];
-        for (int64_t x = P.blk_rng[2 * b]; x < P.blk_rng[2 * b + 1]; ++x) {
-          const int kb = P.blk_kb[x];
-          if (!mbar_wait(smem_u32(&bar_empty[stage]), phase ^ 1, &abort_s)) {
-            fail(1);
-            ok = false;
-            break;
+    // The whole warp loads 32 (A slot, B slot) pairs at a time; lane 0 waits
+    // for free stages and issues the two bulk copies of each.
+    int stage = 0;
+    uint32_t phase = 0;
+    uint32_t issued_parity[STAGES];
+    bool issued[STAGES];
+    for (int s = 0; s < STAGES; ++s) issued[s] = false;
+    bool ok = true;
+    for (int64_t gb = blockIdx.x; gb < nblk_total && ok; gb += gridDim.x) {
+      const int vi = find_view(vstart, nviews, gb);
+      const OzParams& P = views[vi];
+      const int64_t b = gb - vstart[vi];
+      const int64_t x0 = P.blk_rng[2 * b], x1 = P.blk_rng[2 * b + 1];
+      for (int64_t xb = x0; xb < x1 && ok; xb += 32) {
+        int2 mine = make_int2(0, 0);
+        if (xb + lane < x1) mine = P.blk_ab[xb + lane];
+        const int cnt = (int)(x1 - xb < 32 ? x1 - xb : 32);
+        for (int j = 0; j < cnt; ++j) {
+          const int sa = __shfl_sync(0xffffffffu, mine.x, j);
+          const int sb = __shfl_sync(0xffffffffu, mine.y, j);
+          if (lane == 0) {
+            if (!mbar_wait(smem_u32(&bar_empty[stage]), phase ^ 1, &abort_s)) {
+              fail(1);
+              ok = false;
+            } else {
+              uint8_t* dst = stage_base + stage * STAGE_BYTES;
+              const uint32_t full = smem_u32(&bar_full[stage]);
+              mbar_expect_tx(full, STAGE_BYTES);
+              bulk_g2s(smem_u32(dst),
+                       P.Apack + (size_t)(sa - P.a_slot_base) * (S * A_SLICE_BYTES),
+                       S * A_SLICE_BYTES, full);
+              bulk_g2s(smem_u32(dst + S * A_SLICE_BYTES),
+                       P.Bpack + (size_t)sb * (S * B_SLICE_BYTES), S * B_SLICE_BYTES, full);
+              issued[stage] = true;
+              issued_parity[stage] = phase;
+            }
           }
-          const int sa = P.brickA[(int64_t)rb * P.KBn + kb];
-          const int sb = P.brickB[(int64_t)kb * P.CB + cb];
-          uint8_t* dst = stage_base + stage * STAGE_BYTES;
-          const uint32_t full = smem_u32(&bar_full[stage]);
-          mbar_expect_tx(full, STAGE_BYTES);
-          bulk_g2s(smem_u32(dst), P.Apack + (size_t)sa * (S * A_SLICE_BYTES), S * A_SLICE_BYTES,
-                   full);
-          bulk_g2s(smem_u32(dst + S * A_SLICE_BYTES), P.Bpack + (size_t)sb * (S * B_SLICE_BYTES),
-                   S * B_SLICE_BYTES, full);
-          issued[stage] = true;
-          issued_parity[stage] = phase;
+          ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+          if (!ok) break;
           if (++stage == STAGES) {
             stage = 0;
             phase ^= 1;
           }
         }
       }
-      // copies still in flight land before the CTA may exit
+    }
+    // copies still in flight land before the CTA may exit
+    if (lane == 0)
       for (int s = 0; s < STAGES; ++s)
         if (issued[s] && !mbar_wait(smem_u32(&bar_full[s]), issued_parity[s], &abort_s)) {
           const uint64_t t0 = globaltimer();
@@ -299,7 +367,6 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
                  globaltimer() - t0 < WAIT_NS) {
           }
         }
-    }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     // Chunks of CHUNK_STAGES stages start from fresh accumulators; before the
@@ -430,11 +497,12 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
         }
       }
       if (!ok) break;
-      // recombination: C = alpha * 2^(E_A + E_B) * (hi * u3 + lo * u_TOP)
+      // recombination: C = alpha * 2^(E_A + E_B) * (hi * 2^(8(TOP-3)) + lo) * u_TOP,
+      // exact integer to correctly rounded double, then one multiply by alpha
       const int64_t gr = (int64_t)rb * BM + rloc;
       if (gr < P.M_total) {
         const int ti = P.row_tile[gr], lr = P.row_local[gr], ea = P.EA[gr];
-        const double u3 = level_unit(3), ut = level_unit(TOP);
+        const bool unit_alpha = P.alpha == 1.0;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
           const int64_t gc = (int64_t)cb * BN + half * 32 + j;
@@ -442,9 +510,10 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
             const int tj = P.col_tile[gc];
             const int64_t off = P.coff[(int64_t)ti * P.Nt + tj];
             if (off >= 0) {
-              const double v = fma((double)hi[j], u3, (double)lo[j] * ut);
+              const double v = exact_to_double(hi[j], lo[j], 8 * (TOP - 3),
+                                               (2 - 8 * TOP) + (ea - 1022) + (P.EB[gc] - 1022));
               P.C[off + (int64_t)lr * P.nsz[tj] + P.col_local[gc]] =
-                  P.alpha * ldexp(v, (ea - 1022) + (P.EB[gc] - 1022));
+                  unit_alpha ? v : P.alpha * v;
             }
           }
         }
@@ -670,6 +739,22 @@ __global__ void block_list_kernel(const int64_t* __restrict__ counts,
   blk[2 * s + 1] = (int32_t)(x - (x / CB) * CB);
 }
 
+// Brick slots of every (output block, k block): one warp per output block.
+__global__ void slot_pairs_kernel(const int32_t* __restrict__ blk, const int64_t* __restrict__ off,
+                                  int64_t nblk, const int32_t* __restrict__ kbs,
+                                  const int32_t* __restrict__ brickA,
+                                  const int32_t* __restrict__ brickB, int64_t KB, int64_t CB,
+                                  int2* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (b >= nblk) return;
+  const int64_t rb = blk[2 * b], cb = blk[2 * b + 1];
+  for (int64_t x = off[b] + lane; x < off[b + 1]; x += 32) {
+    const int64_t kb = kbs[x];
+    out[x] = make_int2(brickA[rb * KB + kb], brickB[kb * CB + cb]);
+  }
+}
+
 __global__ void flag_nonzero_kernel(const int64_t* __restrict__ counts, int64_t n,
                                     int64_t* __restrict__ flag) {
   const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -710,6 +795,7 @@ struct OzakiPlan {
   std::vector<DevVec> bufs;
   int32_t *row_tile = nullptr, *row_local = nullptr, *k_tile = nullptr, *k_local = nullptr,
           *col_tile = nullptr, *col_local = nullptr, *rstart = nullptr, *cstart = nullptr;
+  int2* blk_ab = nullptr;
   int32_t *EA = nullptr, *EB = nullptr, *brickA = nullptr, *brickB = nullptr, *listA = nullptr,
           *listB = nullptr, *blk = nullptr, *blk_kb = nullptr;
   int64_t *blk_off = nullptr, *blk_rng = nullptr, *workA = nullptr, *workB = nullptr;
@@ -719,6 +805,13 @@ struct OzakiPlan {
   OzParams P{};
   OzParams* d_params = nullptr;   // P on the device (single-view launches)
   int64_t* d_vstart = nullptr;    // {0, nblk}
+  // row chunking: A bricks are built and consumed one range of row blocks at
+  // a time when all of them would not fit next to the operands
+  int nchunk = 1;
+  std::vector<int64_t> chunk_slot{0, 0};   // A slot boundaries
+  std::vector<int64_t> chunk_blk{0, 0};    // block boundaries (scheduling order)
+  OzParams* d_chunk_params = nullptr;
+  int64_t* d_chunk_vstart = nullptr;
   size_t bytes = 0;
   ~OzakiPlan() {
     for (auto& b : bufs)
@@ -766,9 +859,8 @@ void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int
 }
 
 template <int S>
-void launch_split_t(const OzakiPlan& pl, int sm_count, cudaStream_t st) {
-  const int grid_a = (int)std::min<int64_t>(pl.nA, (int64_t)sm_count * 8);
-  const int grid_b = (int)std::min<int64_t>(pl.nB, (int64_t)sm_count * 8);
+void launch_split_t(const OzakiPlan& pl, int sm_count, cudaStream_t st, bool do_a, int64_t a0,
+                    int64_t a1, bool do_b) {
   static bool set = false;
   if (!set) {
     cudaFuncSetAttribute(split_kernel<S, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -777,14 +869,28 @@ void launch_split_t(const OzakiPlan& pl, int sm_count, cudaStream_t st) {
                          S * B_SLICE_BYTES);
     set = true;
   }
-  if (grid_a > 0)
-    split_kernel<S, BM><<<grid_a, 256, S * A_SLICE_BYTES, st>>>(pl.va, pl.row_tile, pl.row_local, pl.k_tile,
-                                                  pl.k_local, pl.EA, pl.M_total, pl.K_total,
-                                                  pl.listA, pl.nA, pl.Apack);
-  if (grid_b > 0)
-    split_kernel<S, BN><<<grid_b, 256, S * B_SLICE_BYTES, st>>>(pl.vb, pl.col_tile, pl.col_local, pl.k_tile,
-                                                  pl.k_local, pl.EB, pl.N_total, pl.K_total,
-                                                  pl.listB, pl.nB, pl.Bpack);
+  const int64_t na = a1 - a0;
+  const int grid_a = (int)std::min<int64_t>(na, (int64_t)sm_count * 8);
+  const int grid_b = (int)std::min<int64_t>(pl.nB, (int64_t)sm_count * 8);
+  if (do_a && grid_a > 0)
+    split_kernel<S, BM><<<grid_a, 256, S * A_SLICE_BYTES, st>>>(
+        pl.va, pl.row_tile, pl.row_local, pl.k_tile, pl.k_local, pl.EA, pl.M_total, pl.K_total,
+        pl.listA + 2 * a0, na, pl.Apack);
+  if (do_b && grid_b > 0)
+    split_kernel<S, BN><<<grid_b, 256, S * B_SLICE_BYTES, st>>>(
+        pl.vb, pl.col_tile, pl.col_local, pl.k_tile, pl.k_local, pl.EB, pl.N_total, pl.K_total,
+        pl.listB, pl.nB, pl.Bpack);
+}
+
+void launch_split(const OzakiPlan& pl, int sm_count, cudaStream_t st, bool do_a, int64_t a0,
+                  int64_t a1, bool do_b) {
+  switch (pl.S) {
+    case 2: launch_split_t<2>(pl, sm_count, st, do_a, a0, a1, do_b); break;
+    case 3: launch_split_t<3>(pl, sm_count, st, do_a, a0, a1, do_b); break;
+    case 4: launch_split_t<4>(pl, sm_count, st, do_a, a0, a1, do_b); break;
+    case 5: launch_split_t<5>(pl, sm_count, st, do_a, a0, a1, do_b); break;
+    default: launch_split_t<6>(pl, sm_count, st, do_a, a0, a1, do_b); break;
+  }
 }
 
 void index_maps(const int32_t* sz, int64_t n, std::vector<int32_t>& tile,
@@ -941,9 +1047,43 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   block_list_kernel<<<blocks_for(nob, 256), 256, 0, s>>>(counts, scan_b, nob, pl->CB, pl->blk);
   gather_offsets_kernel<<<blocks_for(nob, 256), 256, 0, s>>>(counts, scan_c, scan_b, nob,
                                                              pl->blk_off);
-  // Scheduling order: super-tiles of 8 row blocks x 19 column blocks (one
-  // wave of 152 CTAs), so CTAs running together share A bricks (19 ways) and
-  // B bricks (8 ways) in L2.
+  if ((st = pl->alloc(&pl->blk_ab, pl->nkb, err))) return st;
+  if (pl->nblk)
+    slot_pairs_kernel<<<blocks_for(pl->nblk * 32, 256), 256, 0, s>>>(
+        pl->blk, pl->blk_off, pl->nblk, pl->blk_kb, pl->brickA, pl->brickB, pl->KB, pl->CB,
+        pl->blk_ab);
+  // Row chunking: when the A bricks would not fit next to everything else,
+  // they are built and consumed one range of row blocks at a time.
+  const size_t a_brick = (size_t)slices * A_SLICE_BYTES, b_brick = (size_t)slices * B_SLICE_BYTES;
+  std::vector<int64_t> chunk_rb{0, pl->RB};
+  pl->chunk_slot = {0, pl->nA};
+  {
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    size_t budget = free_b / 2;
+    if (const char* e = getenv("TAGPU_OZAKI_A_BYTES")) budget = (size_t)atof(e);
+    budget = std::max<size_t>(budget, a_brick * (size_t)pl->KB);  // at least one row block
+    if (a_brick * (size_t)pl->nA > budget && pl->nA > 0) {
+      std::vector<int32_t> la(2 * pl->nA);
+      cudaMemcpyAsync(la.data(), pl->listA, la.size() * 4, cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+      chunk_rb = {0};
+      pl->chunk_slot = {0};
+      const int64_t per = (int64_t)(budget / a_brick);
+      for (int64_t x = 0; x < pl->nA; ++x) {
+        if (x - pl->chunk_slot.back() >= per && (x == 0 || la[2 * x] != la[2 * (x - 1)])) {
+          pl->chunk_slot.push_back(x);
+          chunk_rb.push_back(la[2 * x]);
+        }
+      }
+      pl->chunk_slot.push_back(pl->nA);
+      chunk_rb.push_back(pl->RB);
+    }
+    pl->nchunk = (int)pl->chunk_slot.size() - 1;
+  }
+  // Scheduling order: chunk first, then super-tiles of 8 row blocks x 19
+  // column blocks (one wave of 152 CTAs), so CTAs running together share A
+  // bricks (19 ways) and B bricks (8 ways) in L2.
   {
     std::vector<int32_t> hb(2 * pl->nblk);
     std::vector<int64_t> ho(pl->nblk + 1);
@@ -954,15 +1094,24 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
     }
     const int64_t GR = 8, GC = 19;
     const int64_t nsc = (pl->CB + GC - 1) / GC;
-    std::vector<std::pair<int64_t, int64_t>> key(pl->nblk);
+    auto chunk_of = [&](int64_t rb) {
+      return (int64_t)(std::upper_bound(chunk_rb.begin(), chunk_rb.end(), rb) - chunk_rb.begin()) -
+             1;
+    };
+    std::vector<std::pair<std::pair<int64_t, int64_t>, int64_t>> key(pl->nblk);
     for (int64_t b = 0; b < pl->nblk; ++b) {
       const int64_t rb = hb[2 * b], cb = hb[2 * b + 1];
       const int64_t tile = (rb / GR) * nsc + cb / GC;
-      key[b] = {tile * GR * GC + (cb % GC) * GR + (rb % GR), b};
+      key[b] = {{chunk_of(rb), tile * GR * GC + (cb % GC) * GR + (rb % GR)}, b};
     }
     std::sort(key.begin(), key.end());
     std::vector<int32_t> nb(2 * pl->nblk);
     std::vector<int64_t> rng(2 * pl->nblk);
+    pl->chunk_blk.assign(pl->nchunk + 1, pl->nblk);
+    pl->chunk_blk[0] = 0;
+    for (int64_t i = pl->nblk - 1; i >= 0; --i) pl->chunk_blk[key[i].first.first] = i;
+    for (int c = pl->nchunk - 1; c >= 0; --c)
+      pl->chunk_blk[c] = std::min(pl->chunk_blk[c], pl->chunk_blk[c + 1]);
     for (int64_t i = 0; i < pl->nblk; ++i) {
       const int64_t b = key[i].second;
       nb[2 * i] = hb[2 * b];
@@ -973,9 +1122,11 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
     if ((st = pl->upload(&pl->blk_rng, rng, err))) return st;
     if (pl->nblk) cudaMemcpyAsync(pl->blk, nb.data(), nb.size() * 4, cudaMemcpyHostToDevice, s);
   }
-  // operand slices
-  const size_t a_brick = (size_t)slices * A_SLICE_BYTES, b_brick = (size_t)slices * B_SLICE_BYTES;
-  if ((st = pl->alloc(&pl->Apack, a_brick * pl->nA, err)) ||
+  // operand slices (A: the largest chunk)
+  int64_t max_slots = 0;
+  for (int c = 0; c < pl->nchunk; ++c)
+    max_slots = std::max(max_slots, pl->chunk_slot[c + 1] - pl->chunk_slot[c]);
+  if ((st = pl->alloc(&pl->Apack, a_brick * max_slots, err)) ||
       (st = pl->alloc(&pl->Bpack, b_brick * pl->nB, err)))
     return st;
   cudaError_t ce = cudaGetLastError();
@@ -990,7 +1141,7 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   P.brickB = pl->brickB;
   P.blk = pl->blk;
   P.blk_rng = pl->blk_rng;
-  P.blk_kb = pl->blk_kb;
+  P.blk_ab = pl->blk_ab;
   P.nblk = pl->nblk;
   P.KBn = (int)pl->KB;
   P.CB = (int)pl->CB;
@@ -1008,6 +1159,25 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   P.M_total = pl->M_total;
   P.N_total = pl->N_total;
   P.err = pl->err;
+  P.a_slot_base = 0;
+  if (pl->nchunk > 1) {
+    std::vector<OzParams> cp(pl->nchunk, P);
+    std::vector<int64_t> cv(2 * pl->nchunk);
+    for (int c = 0; c < pl->nchunk; ++c) {
+      cp[c].blk = P.blk + 2 * pl->chunk_blk[c];
+      cp[c].blk_rng = P.blk_rng + 2 * pl->chunk_blk[c];
+      cp[c].nblk = pl->chunk_blk[c + 1] - pl->chunk_blk[c];
+      cp[c].a_slot_base = pl->chunk_slot[c];
+      cv[2 * c] = 0;
+      cv[2 * c + 1] = cp[c].nblk;
+    }
+    if ((st = pl->alloc(&pl->d_chunk_params, pl->nchunk, err)) ||
+        (st = pl->alloc(&pl->d_chunk_vstart, 2 * pl->nchunk, err)))
+      return st;
+    cudaMemcpyAsync(pl->d_chunk_params, cp.data(), cp.size() * sizeof(OzParams),
+                    cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(pl->d_chunk_vstart, cv.data(), cv.size() * 8, cudaMemcpyHostToDevice, s);
+  }
   if ((st = pl->alloc(&pl->d_params, 1, err)) || (st = pl->alloc(&pl->d_vstart, 2, err)))
     return st;
   const int64_t vs[2] = {0, pl->nblk};
@@ -1029,13 +1199,8 @@ void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s) {
   if (pl->nworkB)
     frame_kernel<<<blocks_for(pl->nworkB * 32, 256), 256, 0, s>>>(pl->vb, pl->cstart, pl->workB,
                                                                    pl->nworkB, pl->EB);
-  switch (pl->S) {
-    case 2: launch_split_t<2>(*pl, sm_count, s); break;
-    case 3: launch_split_t<3>(*pl, sm_count, s); break;
-    case 4: launch_split_t<4>(*pl, sm_count, s); break;
-    case 5: launch_split_t<5>(*pl, sm_count, s); break;
-    default: launch_split_t<6>(*pl, sm_count, s); break;
-  }
+  // chunked plans split A chunk by chunk inside ozaki_enqueue_gemm
+  launch_split(*pl, sm_count, s, pl->nchunk == 1, 0, pl->nA, true);
 }
 
 void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int nviews,
@@ -1052,8 +1217,19 @@ void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int
 }
 
 void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s) {
-  ozaki_enqueue_gemm_views(pl->d_params, pl->d_vstart, 1, pl->nblk, pl->S, pl->err, sm_count, s);
+  if (pl->nchunk == 1) {
+    ozaki_enqueue_gemm_views(pl->d_params, pl->d_vstart, 1, pl->nblk, pl->S, pl->err, sm_count,
+                             s);
+    return;
+  }
+  for (int c = 0; c < pl->nchunk; ++c) {
+    launch_split(*pl, sm_count, s, true, pl->chunk_slot[c], pl->chunk_slot[c + 1], false);
+    ozaki_enqueue_gemm_views(pl->d_chunk_params + c, pl->d_chunk_vstart + 2 * c, 1,
+                             pl->chunk_blk[c + 1] - pl->chunk_blk[c], pl->S, pl->err, sm_count, s);
+  }
 }
+
+int ozaki_chunks(const OzakiPlan* pl) { return pl->nchunk; }
 
 size_t ozaki_params_size() { return sizeof(OzParams); }
 void ozaki_params(const OzakiPlan* pl, void* out) { *static_cast<OzParams*>(out) = pl->P; }

@@ -1351,7 +1351,15 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, Launch
     c->st.gemm_launches = 5;
   }
   for (int S = 2; S < 8; ++S) {
-    auto& g = by_s[S];
+    auto& g0 = by_s[S];
+    std::vector<Contraction*> g;
+    for (auto* c : g0) {
+      if (ozaki_chunks(c->oz) > 1) {
+        ozaki_enqueue_gemm(c->oz, ctx->sm_count, stream);
+      } else {
+        g.push_back(c);
+      }
+    }
     if (g.empty()) continue;
     if (g.size() == 1) {
       ozaki_enqueue_gemm(g[0]->oz, ctx->sm_count, stream);
