@@ -217,10 +217,6 @@ __device__ __forceinline__ double exact_to_double(int64_t hi, int64_t lo, int sh
   return __longlong_as_double((long long)(bits | (neg ? (1ull << 63) : 0)));
 }
 
-// 2^(2 - 8t): the unit of level t (products of digits d_p e_q with p + q = t)
-__device__ __forceinline__ double level_unit(int t) {
-  return __longlong_as_double((long long)(1023 + 2 - 8 * t) << 52);
-}
 
 struct OzParams {
   const uint8_t* Apack;      // A bricks, S * 8 KB each
