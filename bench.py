@@ -34,9 +34,6 @@ sys.path.insert(0, ROOT)
 
 METRIC = "nonzero-block TFLOP/s at <=1e-12 rel err, emulated vs plain FP64; p50/p99 latency"
 SLICE_PAIRS = {s: s * (s + 1) // 2 for s in range(2, 9)}
-# mma.sync m8n8k4 f64 throughput measured on this GPU model (no FP64 figure
-# is among the measured peaks)
-FP64_DMMA_PEAK = 1.04
 
 
 def workload(n=16384, seed=0, lo=48, hi=256, decay=4.0, cut=1e-10):
@@ -514,9 +511,10 @@ def main():
                           f"{pairs_per} per FP64 product)", "peak_kind": f"{peak_kind} bf16 burst"}
     else:
         achieved = flops / (gemm_ms * 1e-3) / 1e12
-        roof = {"bound": "tensor", "achieved": achieved, "peak": FP64_DMMA_PEAK,
-                "unit": "TFLOP/s", "frac": achieved / FP64_DMMA_PEAK, "traffic": None,
-                "kernel": "dmma_gemm", "peak_kind": "measured DMMA (profiles/fp64_peak_gb300.md)"}
+        dmma_peak, _ = w.fp64_rates()
+        roof = {"bound": "tensor", "achieved": achieved, "peak": dmma_peak,
+                "unit": "TFLOP/s", "frac": achieved / dmma_peak, "traffic": None,
+                "kernel": "dmma_gemm", "peak_kind": "measured DMMA rate (tagpu_device_fp64_rates)"}
     out = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -540,9 +538,13 @@ def main():
         Cp, stp = ta.contract(w, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_FP64)
         x, y = C.download(), Cp.download()
         err = float(np.linalg.norm(x - y) / np.linalg.norm(y))
+        dmma_peak, dfma_peak = w.fp64_rates()
         out["plain_fp64"] = {"value": flops / (stp["ms_total"] * 1e-3) / 1e12,
                              "ms_per_step": stp["ms_total"], "ms_gemm": stp["ms_gemm"],
-                             "unit": "TFLOP/s"}
+                             "unit": "TFLOP/s", "dmma_peak_tflops": dmma_peak,
+                             "dfma_peak_tflops": dfma_peak,
+                             "frac_of_dmma_peak": flops / (stp["ms_gemm"] * 1e-3) / 1e12 /
+                             dmma_peak}
         out["rel_err_vs_plain_fp64"] = err
         out["emulated_over_plain"] = value / out["plain_fp64"]["value"]
         del Cp, x, y

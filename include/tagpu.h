@@ -89,6 +89,11 @@ tagpu_status tagpu_sync(tagpu_ctx* ctx);
 tagpu_status tagpu_timer_start(tagpu_ctx* ctx);
 tagpu_status tagpu_timer_stop(tagpu_ctx* ctx, double* ms);
 
+/* Measured FP64 rates of the context's GPU (TFLOP/s): DMMA (mma.sync f64)
+ * and FMA, from short dependent-chain loops (~0.1 s).  No counterpart in the
+ * reference; used as the plain form's roofline denominator. */
+tagpu_status tagpu_device_fp64_rates(tagpu_ctx* ctx, double* dmma_tflops, double* dfma_tflops);
+
 /* Default screening threshold used for new result shapes; initial value is
  * FLT_EPSILON as in SparseShape<float>. */
 float tagpu_threshold_get(const tagpu_ctx* ctx);

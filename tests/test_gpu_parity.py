@@ -212,3 +212,8 @@ def test_all_screened_result(ta, world):
     C, st = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j")
     assert st["nonzero_result_tiles"] == 0 and st["pairs"] == 0
     assert C.info().elements == 0
+
+
+def test_fp64_rates_measured(ta, world):
+    dmma, dfma = world.fp64_rates()
+    assert 0.05 < dmma < 200 and 0.05 < dfma < 200

@@ -120,6 +120,7 @@ SIGNATURES = {
     "tagpu_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "tagpu_sync": (ctypes.c_int, [_vp]),
     "tagpu_timer_start": (ctypes.c_int, [_vp]),
+    "tagpu_device_fp64_rates": (ctypes.c_int, [_vp, _f64p, _f64p]),
     "tagpu_timer_stop": (ctypes.c_int, [_vp, _f64p]),
     "tagpu_threshold_get": (ctypes.c_float, [_vp]),
     "tagpu_threshold_set": (None, [_vp, ctypes.c_float]),
@@ -218,6 +219,12 @@ class World:
 
     def sync(self):
         self.check(self.L.tagpu_sync(self.h))
+
+    def fp64_rates(self):
+        """Measured (DMMA, DFMA) TFLOP/s of this GPU."""
+        a, b = ctypes.c_double(0), ctypes.c_double(0)
+        self.check(self.L.tagpu_device_fp64_rates(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def timer_start(self):
         self.check(self.L.tagpu_timer_start(self.h))

@@ -55,6 +55,10 @@ void launch_permute(cudaStream_t s, const PermuteDesc& d, int64_t ntiles,
 // the kernel's decomposition).
 int64_t permute_items(const PermuteDesc& d, const int64_t* ext);
 
+// FP64 tensor (DMMA) and FMA rates measured with dependent-chain loops.
+tagpu_status measure_fp64_rates(cudaStream_t s, int sm_count, double* dmma_tflops,
+                                double* dfma_tflops);
+
 // Generation of synthetic operands and sequential tile norms.
 struct GenDesc {
   int rank;

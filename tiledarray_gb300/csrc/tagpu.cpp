@@ -546,6 +546,15 @@ tagpu_status tagpu_timer_stop(tagpu_ctx* ctx, double* ms) {
   return TAGPU_OK;
 }
 
+tagpu_status tagpu_device_fp64_rates(tagpu_ctx* ctx, double* dmma_tflops, double* dfma_tflops) {
+  if (!ctx || !dmma_tflops || !dfma_tflops) return TAGPU_ERR_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  tagpu_status st = measure_fp64_rates(ctx->stream, ctx->sm_count, dmma_tflops, dfma_tflops);
+  if (st) return fail(ctx, st, "FP64 rate measurement failed");
+  return TAGPU_OK;
+}
+
 float tagpu_threshold_get(const tagpu_ctx* ctx) { return ctx ? ctx->threshold : 0.0f; }
 void tagpu_threshold_set(tagpu_ctx* ctx, float t) {
   if (ctx) ctx->threshold = t;
