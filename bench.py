@@ -532,7 +532,7 @@ def main():
            "latency_ms": {"p50": p50, "p99": p99},
            "phases_ms": {k: stats[k] for k in ("ms_shape", "ms_pairs", "ms_split", "ms_gemm")},
            "roofline": roof, "clocks": clocks,
-           "gpu_launches": int(4 + stats["gemm_launches"])}
+           "gpu_launches": int(stats["kernel_launches"])}
     # error vs plain FP64 (DMMA) on the device, and the plain form's speed
     if rank == 0 and not args.no_plain and prec == ta.PRECISION_OZAKI:
         Cp, stp = ta.contract(w, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_FP64)

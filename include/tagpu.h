@@ -174,7 +174,8 @@ typedef struct tagpu_contract_stats {
   int precision;
   int slices;
   int64_t gemm_blocks;        /* output blocks the GEMM ran */
-  int64_t gemm_launches;      /* kernels launched by the call */
+  int64_t gemm_launches;      /* GEMM-phase kernel launches */
+  int64_t kernel_launches;    /* every kernel the call launched */
 } tagpu_contract_stats;
 
 /* c = alpha * A(a_idx) * B(b_idx) with index strings like "i,k".  *c is a new

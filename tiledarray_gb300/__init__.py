@@ -71,7 +71,7 @@ class ContractStats(ctypes.Structure):
                 ("ms_total", ctypes.c_double), ("left_permtype", ctypes.c_int),
                 ("right_permtype", ctypes.c_int), ("precision", ctypes.c_int),
                 ("slices", ctypes.c_int), ("gemm_blocks", ctypes.c_int64),
-                ("gemm_launches", ctypes.c_int64)]
+                ("gemm_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

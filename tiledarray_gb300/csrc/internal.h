@@ -12,6 +12,10 @@
 
 namespace tagpu {
 
+// Kernel launches made by this library (every launch site counts itself).
+void count_launch();
+int64_t launch_count();
+
 // Record a message as the context's last error and return `st`.
 tagpu_status set_last_error(tagpu_ctx* ctx, tagpu_status st, const char* msg);
 // Device ordinal of a context.

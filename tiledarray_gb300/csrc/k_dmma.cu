@@ -174,6 +174,7 @@ void launch_dmma_gemm(cudaStream_t s, const GemmView* views, const WorkItem* ite
   }
   const int64_t grid = nitems < (int64_t)sm_count * per_sm ? nitems : (int64_t)sm_count * per_sm;
   dmma_gemm_kernel<<<(unsigned)grid, 128, smem, s>>>(views, items, nitems);
+  count_launch();
 }
 
 }  // namespace tagpu

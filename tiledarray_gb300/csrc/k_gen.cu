@@ -84,6 +84,7 @@ void launch_generate(cudaStream_t s, const GenDesc& g, int64_t ntiles,
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   generate_kernel<<<sms * 8, 256, 0, s>>>(g, ntiles, tile_lo, tile_ext, tile_off, tile_scale,
                                           data);
+  count_launch();
 }
 
 void launch_tile_norms(cudaStream_t s, int64_t ntiles, const int64_t* tile_off,
@@ -92,6 +93,7 @@ void launch_tile_norms(cudaStream_t s, int64_t ntiles, const int64_t* tile_off,
   const int threads = 64;
   tile_norms_kernel<<<(unsigned)((ntiles + threads - 1) / threads), threads, 0, s>>>(
       ntiles, tile_off, data, norms);
+  count_launch();
 }
 
 }  // namespace tagpu

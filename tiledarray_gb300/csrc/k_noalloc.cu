@@ -98,6 +98,7 @@ extern "C" tagpu_status tagpu_pair_list_noalloc(tagpu_ctx* ctx, int64_t M, int64
     const int threads = 256;
     noalloc_count_kernel<<<(unsigned)((MN * 32 + threads - 1) / threads), threads, 0, s>>>(
         M, N, K, cnorm, c_thr, lnorm, l_thr, rnorm, r_thr, counts);
+    count_launch();
   }
   launch_exclusive_scan(s, counts, MN, offsets);
   int64_t np = 0;

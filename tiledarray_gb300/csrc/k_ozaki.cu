@@ -852,6 +852,7 @@ void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int
   const int64_t grid = std::min<int64_t>(nblk, sm_count);
   if (grid > 0)
     ozaki_gemm_kernel<S><<<(unsigned)grid, THREADS, smem, st>>>(views, vstart, nviews, nblk, err);
+    count_launch();
 }
 
 template <int S>
@@ -872,10 +873,12 @@ void launch_split_t(const OzakiPlan& pl, int sm_count, cudaStream_t st, bool do_
     split_kernel<S, BM><<<grid_a, 256, S * A_SLICE_BYTES, st>>>(
         pl.va, pl.row_tile, pl.row_local, pl.k_tile, pl.k_local, pl.EA, pl.M_total, pl.K_total,
         pl.listA + 2 * a0, na, pl.Apack);
+    count_launch();
   if (do_b && grid_b > 0)
     split_kernel<S, BN><<<grid_b, 256, S * B_SLICE_BYTES, st>>>(
         pl.vb, pl.col_tile, pl.col_local, pl.k_tile, pl.k_local, pl.EB, pl.N_total, pl.K_total,
         pl.listB, pl.nB, pl.Bpack);
+    count_launch();
 }
 
 void launch_split(const OzakiPlan& pl, int sm_count, cudaStream_t st, bool do_a, int64_t a0,
@@ -993,9 +996,11 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
     return st;
   brick_flag_kernel<<<blocks_for(nfa, 256), 256, 0, s>>>(a, pl->row_tile, pl->k_tile, pl->M_total,
                                                          pl->K_total, BM, pl->RB, pl->KB, flag);
+  count_launch();
   launch_exclusive_scan(s, flag, nfa, scan);
   brick_slot_kernel<<<blocks_for(nfa, 256), 256, 0, s>>>(flag, scan, nfa, pl->KB, pl->brickA,
                                                          pl->listA);
+  count_launch();
   cudaMemcpyAsync(&pl->nA, scan + nfa, 8, cudaMemcpyDeviceToHost, s);
   cudaStreamSynchronize(s);
   // B bricks are indexed (k block, column block) in the GEMM; the flag pass
@@ -1006,9 +1011,11 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
     brick_flag_kernel<<<blocks_for(nfb, 256), 256, 0, s>>>(b, pl->col_tile, pl->k_tile,
                                                            pl->N_total, pl->K_total, BN, pl->CB,
                                                            pl->KB, flag);
+    count_launch();
     launch_exclusive_scan(s, flag, nfb, scan);
     brick_slot_kernel<<<blocks_for(nfb, 256), 256, 0, s>>>(flag, scan, nfb, pl->KB, slot_cb,
                                                            pl->listB);
+    count_launch();
     cudaMemcpyAsync(&pl->nB, scan + nfb, 8, cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
     std::vector<int32_t> h(nfb), t(nfb);
@@ -1027,8 +1034,10 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   block_kernel<<<blocks_for(nob * 32, 256), 256, 0, s>>>(
       pl->brickA, pl->brickB, pl->row_tile, pl->col_tile, v.coff, v.Nt, pl->M_total, pl->N_total,
       pl->RB, pl->CB, pl->KB, nullptr, counts, nullptr);
+  count_launch();
   launch_exclusive_scan(s, counts, nob, scan_c);
   flag_nonzero_kernel<<<blocks_for(nob, 256), 256, 0, s>>>(counts, nob, bflag);
+  count_launch();
   launch_exclusive_scan(s, bflag, nob, scan_b);
   cudaMemcpyAsync(&pl->nkb, scan_c + nob, 8, cudaMemcpyDeviceToHost, s);
   cudaMemcpyAsync(&pl->nblk, scan_b + nob, 8, cudaMemcpyDeviceToHost, s);
@@ -1040,14 +1049,18 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   block_kernel<<<blocks_for(nob * 32, 256), 256, 0, s>>>(
       pl->brickA, pl->brickB, pl->row_tile, pl->col_tile, v.coff, v.Nt, pl->M_total, pl->N_total,
       pl->RB, pl->CB, pl->KB, scan_c, counts, pl->blk_kb);
+  count_launch();
   block_list_kernel<<<blocks_for(nob, 256), 256, 0, s>>>(counts, scan_b, nob, pl->CB, pl->blk);
+  count_launch();
   gather_offsets_kernel<<<blocks_for(nob, 256), 256, 0, s>>>(counts, scan_c, scan_b, nob,
                                                              pl->blk_off);
+  count_launch();
   if ((st = pl->alloc(&pl->blk_ab, pl->nkb, err))) return st;
   if (pl->nblk)
     slot_pairs_kernel<<<blocks_for(pl->nblk * 32, 256), 256, 0, s>>>(
         pl->blk, pl->blk_off, pl->nblk, pl->blk_kb, pl->brickA, pl->brickB, pl->KB, pl->CB,
         pl->blk_ab);
+    count_launch();
   // Row chunking: when the A bricks would not fit next to everything else,
   // they are built and consumed one range of row blocks at a time.
   const size_t a_brick = (size_t)slices * A_SLICE_BYTES, b_brick = (size_t)slices * B_SLICE_BYTES;
@@ -1192,9 +1205,11 @@ void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s) {
   if (pl->nworkA)
     frame_kernel<<<blocks_for(pl->nworkA * 32, 256), 256, 0, s>>>(pl->va, pl->rstart, pl->workA,
                                                                    pl->nworkA, pl->EA);
+    count_launch();
   if (pl->nworkB)
     frame_kernel<<<blocks_for(pl->nworkB * 32, 256), 256, 0, s>>>(pl->vb, pl->cstart, pl->workB,
                                                                    pl->nworkB, pl->EB);
+    count_launch();
   // chunked plans split A chunk by chunk inside ozaki_enqueue_gemm
   launch_split(*pl, sm_count, s, pl->nchunk == 1, 0, pl->nA, true);
 }

@@ -54,12 +54,14 @@ tagpu_status measure_fp64_rates(cudaStream_t s, int sm_count, double* dmma_tflop
     float ms = 0;
     cudaEventRecord(e0, s);
     dmma_rate_kernel<<<blocks, threads, 0, s>>>(out, iters);
+    count_launch();
     cudaEventRecord(e1, s);
     cudaEventSynchronize(e1);
     cudaEventElapsedTime(&ms, e0, e1);
     if (ms < best_mma) best_mma = ms;
     cudaEventRecord(e0, s);
     dfma_rate_kernel<<<blocks, threads, 0, s>>>(out, iters);
+    count_launch();
     cudaEventRecord(e1, s);
     cudaEventSynchronize(e1);
     cudaEventElapsedTime(&ms, e0, e1);

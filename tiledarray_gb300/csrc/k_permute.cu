@@ -158,6 +158,7 @@ void launch_permute(cudaStream_t s, const PermuteDesc& d, int64_t ntiles,
   const int64_t grid = nitems < (int64_t)sms * 16 ? nitems : (int64_t)sms * 16;
   permute_kernel<<<(unsigned)grid, 256, 0, s>>>(d, ntiles, ext, in_off, out_off, item_start,
                                                 nitems, in, out);
+  count_launch();
 }
 
 }  // namespace tagpu

@@ -160,6 +160,7 @@ void launch_shape_gemm(cudaStream_t s, int64_t M, int64_t N, int64_t K,
   const int64_t blocks = (total + threads - 1) / threads;
   shape_gemm_kernel<<<(unsigned)blocks, threads, 0, s>>>(M, N, K, L, R, ksz, abs_factor,
                                                          thr, C, zero_count);
+  count_launch();
 }
 
 void launch_pair_count(cudaStream_t s, int64_t M, int64_t N, int64_t K,
@@ -173,10 +174,12 @@ void launch_pair_count(cudaStream_t s, int64_t M, int64_t N, int64_t K,
   const int64_t blocks = (total * 32 + threads - 1) / threads;
   pair_count_kernel<<<(unsigned)blocks, threads, 0, s>>>(M, N, K, C, cthr, L, lthr, R, rthr,
                                                          msz, nsz, ksz, counts, flops);
+  count_launch();
 }
 
 void launch_exclusive_scan(cudaStream_t s, const int64_t* in, int64_t n, int64_t* out) {
   exclusive_scan_kernel<<<1, 1024, 0, s>>>(in, n, out);
+  count_launch();
 }
 
 void launch_pair_emit(cudaStream_t s, int64_t M, int64_t N, int64_t K,
@@ -189,6 +192,7 @@ void launch_pair_emit(cudaStream_t s, int64_t M, int64_t N, int64_t K,
   const int64_t blocks = (total * 32 + threads - 1) / threads;
   pair_emit_kernel<<<(unsigned)blocks, threads, 0, s>>>(M, N, K, C, cthr, L, lthr, R, rthr,
                                                         offsets, kidx);
+  count_launch();
 }
 
 }  // namespace tagpu

@@ -141,6 +141,10 @@ tagpu_array::~tagpu_array() {
 }
 
 namespace tagpu {
+static std::atomic<int64_t> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
 tagpu_status set_last_error(tagpu_ctx* ctx, tagpu_status st, const char* msg) {
   if (ctx) ctx->err = msg;
   return st;
@@ -1411,6 +1415,7 @@ tagpu_status contract_impl(tagpu_ctx* ctx, const char* c_idx, double alpha, tagp
                            const tagpu_contract_opts* opts, tagpu_array** out,
                            tagpu_contract_stats* stats) {
   const auto t0 = std::chrono::steady_clock::now();
+  const int64_t launches0 = launch_count();
   Contraction c(ctx);
   tagpu_status e = plan_all(c, c_idx, alpha, A, a_idx, B, b_idx, opts);
   if (e) return e;
@@ -1441,6 +1446,7 @@ tagpu_status contract_impl(tagpu_ctx* ctx, const char* c_idx, double alpha, tagp
     c.st.ms_gemm = tm.ms();
   }
   fill_stats(c);
+  c.st.kernel_launches = launch_count() - launches0;
   c.st.ms_total =
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (stats) *stats = c.st;
