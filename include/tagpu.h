@@ -156,6 +156,12 @@ typedef struct tagpu_contract_opts {
   int precision;              /* tagpu_precision */
   int slices;                 /* Ozaki slices per operand, 2..6, 0 = default (6) */
   float threshold;            /* result screening threshold, <0 = default */
+  int autotune;               /* emulated form: time the GEMM schedules (block
+                                 order, accumulation chunk) on first use of a
+                                 shape bucket and cache the fastest in the file
+                                 named by TAGPU_TUNE_CACHE (results do not
+                                 depend on the schedule); also enabled by the
+                                 environment variable TAGPU_AUTOTUNE=1 */
 } tagpu_contract_opts;
 
 typedef struct tagpu_contract_stats {

@@ -214,7 +214,9 @@ class DistArray {
     precision_ = p;
     slices_ = slices;
   }
-  tagpu_contract_opts opts() const { return tagpu_contract_opts{precision_, slices_, -1.0f}; }
+  tagpu_contract_opts opts() const {
+    return tagpu_contract_opts{precision_, slices_, -1.0f, 0};
+  }
   void reset(tagpu_array* a, World* w = nullptr) {
     if (w) world_ = w;
     h_.reset(a, [](tagpu_array* x) { tagpu_array_destroy(x); });

@@ -150,3 +150,23 @@ def test_ozaki_row_chunking_identical(ta, world, monkeypatch):
     monkeypatch.setenv("TAGPU_OZAKI_A_BYTES", str(3 * 6 * 8192 * 40))
     got, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI)
     assert np.array_equal(got.download(), ref.download())
+
+
+def test_ozaki_autotune_identical_and_cached(ta, world, tmp_path, monkeypatch):
+    """The autotuner only changes the schedule: results are bit-identical; the
+    chosen schedule is cached per shape bucket."""
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("TAGPU_TUNE_CACHE", str(cache))
+    h = uneven(900, 48, 200, 31)
+    A, _ = gpu_operand(ta, world, [h, h], 8, 0, kind=0)
+    B, _ = gpu_operand(ta, world, [h, h], 8, 1, kind=0)
+    ref, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI)
+    got, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI,
+                         autotune=True)
+    assert np.array_equal(got.download(), ref.download())
+    lines = cache.read_text().split("\n")
+    assert lines[0].startswith("S6_") and len(lines[0].split()) == 5
+    again, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI,
+                           autotune=True)
+    assert np.array_equal(again.download(), ref.download())
+    assert len([x for x in cache.read_text().split("\n") if x]) == 1

@@ -59,7 +59,7 @@ class ArrayInfo(ctypes.Structure):
 
 class ContractOpts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("slices", ctypes.c_int),
-                ("threshold", ctypes.c_float)]
+                ("threshold", ctypes.c_float), ("autotune", ctypes.c_int)]
 
 
 class ContractStats(ctypes.Structure):
@@ -476,7 +476,7 @@ class DistArray:
     def __setitem__(self, indices: str, expr):
         if not isinstance(expr, MultExpr):
             raise TypeError("only contractions A(...) * B(...) are on this path")
-        opts = ContractOpts(self.precision, self.slices, -1.0)
+        opts = ContractOpts(self.precision, self.slices, -1.0, 0)
         h = _vp()
         W = self.world
         W.check(W.L.tagpu_contract(W.h, indices.encode(), float(expr.factor), expr.left.array.h,
@@ -497,10 +497,10 @@ def TArrayD(world, trange=None, **kw):
 
 
 def contract(world, c_idx, alpha, A, a_idx, B, b_idx, precision=PRECISION_FP64, slices=0,
-             threshold=-1.0):
+             threshold=-1.0, autotune=False):
     """Functional form of C(c_idx) = alpha * A(a_idx) * B(b_idx); returns
     (result DistArray, stats dict)."""
-    opts = ContractOpts(precision, slices, threshold)
+    opts = ContractOpts(precision, slices, threshold, int(autotune))
     h = _vp()
     world.check(world.L.tagpu_contract(world.h, c_idx.encode(), float(alpha), A.h,
                                        a_idx.encode(), B.h, b_idx.encode(), ctypes.byref(opts),

@@ -125,6 +125,10 @@ void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int
 // Number of row chunks (1 unless the A digit bricks would not fit at once;
 // chunked plans are launched on their own, not grouped with others).
 int ozaki_chunks(const OzakiPlan* pl);
+// Times the block-order and chunk schedules on this contraction and applies
+// the fastest; cache: file of tuned buckets (NULL or "" = no cache).
+tagpu_status ozaki_autotune(OzakiPlan* pl, int sm_count, cudaStream_t s, const char* cache,
+                            std::string* log, std::string* err);
 size_t ozaki_params_size();
 void ozaki_params(const OzakiPlan* pl, void* out);
 int ozaki_slices(const OzakiPlan* pl);

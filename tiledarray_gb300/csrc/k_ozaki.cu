@@ -53,7 +53,10 @@ namespace {
 constexpr int BM = 128;            // output block rows (MMA M)
 constexpr int BN = 64;             // output block columns (MMA N)
 constexpr int BK = 32;             // k per stage (two MMA K = 16 steps)
-constexpr int CHUNK_STAGES = 4;    // fresh accumulators every 128 k (exact fp32 sums)
+// Fresh accumulators every chunk of `chunk` stages (32 k each).  Exactness
+// bound: level S+1 collects S products of |d e| <= 2^14 per k, so
+// S * 32 * chunk * 2^14 < 2^24, i.e. chunk <= max_chunk(S).
+__host__ __device__ constexpr int max_chunk(int S) { return (1 << 24) / (S * 32 * (1 << 14)); }
 constexpr int A_SLICE_BYTES = BM * BK * 2;   // 8 KB
 constexpr int B_SLICE_BYTES = BN * BK * 2;   // 4 KB
 constexpr int EPI_WARPS = 8;
@@ -242,6 +245,7 @@ struct OzParams {
   double* C;
   int64_t M_total, N_total;
   int* err;                  // error flag (0 = ok)
+  int chunk;                 // stages per accumulation chunk (<= max_chunk(S))
 };
 
 template <int S>
@@ -365,7 +369,7 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
         }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
-    // Chunks of CHUNK_STAGES stages start from fresh accumulators; before the
+    // Chunks of P.chunk stages start from fresh accumulators; before the
     // first MMA of a chunk into level t, the epilogue must have drained level
     // t of the previous chunk.  Levels are issued from the top down, the order
     // in which the epilogue drains them.
@@ -379,8 +383,8 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
       const int64_t b = gb - vstart[vi];
       const int64_t n = P.blk_rng[2 * b + 1] - P.blk_rng[2 * b];
       for (int64_t x = 0; x < n && ok; ++x) {
-        const bool chunk_start = (x % CHUNK_STAGES) == 0;
-        const bool chunk_end = ((x + 1) % CHUNK_STAGES) == 0 || x == n - 1;
+        const bool chunk_start = (x % P.chunk) == 0;
+        const bool chunk_end = ((x + 1) % P.chunk) == 0 || x == n - 1;
         if (!mbar_wait(smem_u32(&bar_full[stage]), phase, &abort_s)) {
           fail(2);
           ok = false;
@@ -459,7 +463,7 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
       const int64_t b = gb - vstart[vi];
       const int rb = P.blk[2 * b], cb = P.blk[2 * b + 1];
       const int64_t n = P.blk_rng[2 * b + 1] - P.blk_rng[2 * b];
-      const int64_t nchunks = (n + CHUNK_STAGES - 1) / CHUNK_STAGES;
+      const int64_t nchunks = (n + P.chunk - 1) / P.chunk;
       for (int64_t c = 0; c < nchunks; ++c, ++chunk) {
         if (!mbar_wait(smem_u32(&bar_acc_full), (uint32_t)(chunk & 1), &abort_s)) {
           fail(4);
@@ -808,6 +812,12 @@ struct OzakiPlan {
   std::vector<int64_t> chunk_blk{0, 0};    // block boundaries (scheduling order)
   OzParams* d_chunk_params = nullptr;
   int64_t* d_chunk_vstart = nullptr;
+  std::vector<int64_t> chunk_rb{0, 0};     // row-block boundaries of the chunks
+  // schedule (results do not depend on it): super-tile of the block order and
+  // stages per accumulation chunk
+  int tune_gr = 8, tune_gc = 19, tune_chunk = 4;
+  std::vector<int32_t> h_blk;              // blocks (rb, cb) in discovery order
+  std::vector<int64_t> h_off;              // their k-list offsets
   size_t bytes = 0;
   ~OzakiPlan() {
     for (auto& b : bufs)
@@ -907,6 +917,79 @@ void index_maps(const int32_t* sz, int64_t n, std::vector<int32_t>& tile,
 }
 
 }  // namespace
+
+// Scheduling order of the output blocks and the accumulation chunk length.
+// Blocks are sorted by row chunk, then by super-tiles of gr row blocks x gc
+// column blocks (with 152 CTAs, 8 x 19 is one wave), so CTAs running together
+// share A bricks (gc ways) and B bricks (gr ways) in L2.  Results do not
+// depend on the schedule: every sum is exact.
+tagpu_status ozaki_schedule(OzakiPlan* pl, int gr, int gc, int chunk, std::string* err) {
+  if (gr < 1 || gc < 1 || chunk < 1 || chunk > max_chunk(pl->S)) {
+    *err = "bad emulated-form schedule";
+    return TAGPU_ERR_INVALID;
+  }
+  cudaStream_t s = pl->s;
+  pl->tune_gr = gr;
+  pl->tune_gc = gc;
+  pl->tune_chunk = chunk;
+  const auto& hb = pl->h_blk;
+  const auto& ho = pl->h_off;
+  const int64_t nsc = (pl->CB + gc - 1) / gc;
+  const auto& crb = pl->chunk_rb;
+  auto chunk_of = [&](int64_t rb) {
+    return (int64_t)(std::upper_bound(crb.begin(), crb.end(), rb) - crb.begin()) - 1;
+  };
+  std::vector<std::pair<std::pair<int64_t, int64_t>, int64_t>> key(pl->nblk);
+  for (int64_t b = 0; b < pl->nblk; ++b) {
+    const int64_t rb = hb[2 * b], cb = hb[2 * b + 1];
+    const int64_t tile = (rb / gr) * nsc + cb / gc;
+    key[b] = {{chunk_of(rb), tile * gr * gc + (cb % gc) * gr + (rb % gr)}, b};
+  }
+  std::sort(key.begin(), key.end());
+  std::vector<int32_t> nb(2 * pl->nblk);
+  std::vector<int64_t> rng(2 * pl->nblk);
+  pl->chunk_blk.assign(pl->nchunk + 1, pl->nblk);
+  for (int64_t i = pl->nblk - 1; i >= 0; --i) pl->chunk_blk[key[i].first.first] = i;
+  for (int c = pl->nchunk - 1; c >= 0; --c)
+    pl->chunk_blk[c] = std::min(pl->chunk_blk[c], pl->chunk_blk[c + 1]);
+  for (int64_t i = 0; i < pl->nblk; ++i) {
+    const int64_t b = key[i].second;
+    nb[2 * i] = hb[2 * b];
+    nb[2 * i + 1] = hb[2 * b + 1];
+    rng[2 * i] = ho[b];
+    rng[2 * i + 1] = ho[b + 1];
+  }
+  if (pl->nblk) {
+    cudaMemcpyAsync(pl->blk, nb.data(), nb.size() * 4, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(pl->blk_rng, rng.data(), rng.size() * 8, cudaMemcpyHostToDevice, s);
+  }
+  // the slot pairs follow the k lists, which did not move
+  pl->P.chunk = chunk;
+  if (pl->nchunk > 1) {
+    std::vector<OzParams> cp(pl->nchunk, pl->P);
+    std::vector<int64_t> cv(2 * pl->nchunk);
+    for (int c = 0; c < pl->nchunk; ++c) {
+      cp[c].blk = pl->P.blk + 2 * pl->chunk_blk[c];
+      cp[c].blk_rng = pl->P.blk_rng + 2 * pl->chunk_blk[c];
+      cp[c].nblk = pl->chunk_blk[c + 1] - pl->chunk_blk[c];
+      cp[c].a_slot_base = pl->chunk_slot[c];
+      cv[2 * c] = 0;
+      cv[2 * c + 1] = cp[c].nblk;
+    }
+    cudaMemcpyAsync(pl->d_chunk_params, cp.data(), cp.size() * sizeof(OzParams),
+                    cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(pl->d_chunk_vstart, cv.data(), cv.size() * 8, cudaMemcpyHostToDevice, s);
+  }
+  const int64_t vs[2] = {0, pl->nblk};
+  cudaMemcpyAsync(pl->d_params, &pl->P, sizeof(OzParams), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(pl->d_vstart, vs, sizeof(vs), cudaMemcpyHostToDevice, s);
+  const cudaError_t ce = cudaStreamSynchronize(s);
+  if (ce != cudaSuccess) {
+    *err = std::string("ozaki schedule: ") + cudaGetErrorString(ce);
+    return TAGPU_ERR_CUDA;
+  }
+  return TAGPU_OK;
+}
 
 // Plan: index maps, brick maps, block lists, scratch.  Host reads back only
 // the counts that size the allocations.
@@ -1090,47 +1173,17 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
     }
     pl->nchunk = (int)pl->chunk_slot.size() - 1;
   }
-  // Scheduling order: chunk first, then super-tiles of 8 row blocks x 19
-  // column blocks (one wave of 152 CTAs), so CTAs running together share A
-  // bricks (19 ways) and B bricks (8 ways) in L2.
-  {
-    std::vector<int32_t> hb(2 * pl->nblk);
-    std::vector<int64_t> ho(pl->nblk + 1);
-    if (pl->nblk) {
-      cudaMemcpyAsync(hb.data(), pl->blk, hb.size() * 4, cudaMemcpyDeviceToHost, s);
-      cudaMemcpyAsync(ho.data(), pl->blk_off, ho.size() * 8, cudaMemcpyDeviceToHost, s);
-      cudaStreamSynchronize(s);
-    }
-    const int64_t GR = 8, GC = 19;
-    const int64_t nsc = (pl->CB + GC - 1) / GC;
-    auto chunk_of = [&](int64_t rb) {
-      return (int64_t)(std::upper_bound(chunk_rb.begin(), chunk_rb.end(), rb) - chunk_rb.begin()) -
-             1;
-    };
-    std::vector<std::pair<std::pair<int64_t, int64_t>, int64_t>> key(pl->nblk);
-    for (int64_t b = 0; b < pl->nblk; ++b) {
-      const int64_t rb = hb[2 * b], cb = hb[2 * b + 1];
-      const int64_t tile = (rb / GR) * nsc + cb / GC;
-      key[b] = {{chunk_of(rb), tile * GR * GC + (cb % GC) * GR + (rb % GR)}, b};
-    }
-    std::sort(key.begin(), key.end());
-    std::vector<int32_t> nb(2 * pl->nblk);
-    std::vector<int64_t> rng(2 * pl->nblk);
-    pl->chunk_blk.assign(pl->nchunk + 1, pl->nblk);
-    pl->chunk_blk[0] = 0;
-    for (int64_t i = pl->nblk - 1; i >= 0; --i) pl->chunk_blk[key[i].first.first] = i;
-    for (int c = pl->nchunk - 1; c >= 0; --c)
-      pl->chunk_blk[c] = std::min(pl->chunk_blk[c], pl->chunk_blk[c + 1]);
-    for (int64_t i = 0; i < pl->nblk; ++i) {
-      const int64_t b = key[i].second;
-      nb[2 * i] = hb[2 * b];
-      nb[2 * i + 1] = hb[2 * b + 1];
-      rng[2 * i] = ho[b];
-      rng[2 * i + 1] = ho[b + 1];
-    }
-    if ((st = pl->upload(&pl->blk_rng, rng, err))) return st;
-    if (pl->nblk) cudaMemcpyAsync(pl->blk, nb.data(), nb.size() * 4, cudaMemcpyHostToDevice, s);
+  pl->chunk_rb = chunk_rb;
+  pl->h_blk.resize(2 * pl->nblk);
+  pl->h_off.resize(pl->nblk + 1);
+  if (pl->nblk) {
+    cudaMemcpyAsync(pl->h_blk.data(), pl->blk, pl->h_blk.size() * 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(pl->h_off.data(), pl->blk_off, pl->h_off.size() * 8, cudaMemcpyDeviceToHost,
+                    s);
+    cudaStreamSynchronize(s);
   }
+  if ((st = pl->alloc(&pl->blk_rng, 2 * pl->nblk, err))) return st;
+  pl->tune_chunk = std::min(4, max_chunk(slices));
   // operand slices (A: the largest chunk)
   int64_t max_slots = 0;
   for (int c = 0; c < pl->nchunk; ++c)
@@ -1169,30 +1222,12 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   P.N_total = pl->N_total;
   P.err = pl->err;
   P.a_slot_base = 0;
-  if (pl->nchunk > 1) {
-    std::vector<OzParams> cp(pl->nchunk, P);
-    std::vector<int64_t> cv(2 * pl->nchunk);
-    for (int c = 0; c < pl->nchunk; ++c) {
-      cp[c].blk = P.blk + 2 * pl->chunk_blk[c];
-      cp[c].blk_rng = P.blk_rng + 2 * pl->chunk_blk[c];
-      cp[c].nblk = pl->chunk_blk[c + 1] - pl->chunk_blk[c];
-      cp[c].a_slot_base = pl->chunk_slot[c];
-      cv[2 * c] = 0;
-      cv[2 * c + 1] = cp[c].nblk;
-    }
-    if ((st = pl->alloc(&pl->d_chunk_params, pl->nchunk, err)) ||
-        (st = pl->alloc(&pl->d_chunk_vstart, 2 * pl->nchunk, err)))
-      return st;
-    cudaMemcpyAsync(pl->d_chunk_params, cp.data(), cp.size() * sizeof(OzParams),
-                    cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(pl->d_chunk_vstart, cv.data(), cv.size() * 8, cudaMemcpyHostToDevice, s);
-  }
+  if (pl->nchunk > 1 && ((st = pl->alloc(&pl->d_chunk_params, pl->nchunk, err)) ||
+                         (st = pl->alloc(&pl->d_chunk_vstart, 2 * pl->nchunk, err))))
+    return st;
   if ((st = pl->alloc(&pl->d_params, 1, err)) || (st = pl->alloc(&pl->d_vstart, 2, err)))
     return st;
-  const int64_t vs[2] = {0, pl->nblk};
-  cudaMemcpyAsync(pl->d_params, &P, sizeof(OzParams), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(pl->d_vstart, vs, sizeof(vs), cudaMemcpyHostToDevice, s);
-  cudaStreamSynchronize(s);
+  if ((st = ozaki_schedule(pl.get(), pl->tune_gr, pl->tune_gc, pl->tune_chunk, err))) return st;
   *out = pl.release();
   return TAGPU_OK;
 }
@@ -1241,6 +1276,94 @@ void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s) {
 }
 
 int ozaki_chunks(const OzakiPlan* pl) { return pl->nchunk; }
+
+// Autotuner: times the schedules of the emulated GEMM on the contraction
+// itself (frames and digit bricks built once), keeps the fastest, and caches
+// the choice per shape bucket (slices, log2 of the fused extents, density
+// decile) in a text file, one "bucket gr gc chunk ms" line per bucket.
+namespace {
+std::string tune_bucket(const OzakiPlan* pl) {
+  auto l2 = [](int64_t x) {
+    int b = 0;
+    while ((int64_t(1) << (b + 1)) <= x) ++b;
+    return b;
+  };
+  const double dens = pl->nblk ? (double)pl->nkb / ((double)pl->nblk * (double)pl->KB) : 0.0;
+  char buf[128];
+  snprintf(buf, sizeof(buf), "S%d_M%d_N%d_K%d_d%d", pl->S, l2(pl->M_total), l2(pl->N_total),
+           l2(pl->K_total), (int)(dens * 10));
+  return buf;
+}
+}  // namespace
+
+tagpu_status ozaki_autotune(OzakiPlan* pl, int sm_count, cudaStream_t s, const char* cache,
+                            std::string* log, std::string* err) {
+  const std::string key = tune_bucket(pl);
+  if (cache && *cache) {
+    if (FILE* f = fopen(cache, "r")) {
+      char k[128];
+      int gr, gc, ch;
+      double ms;
+      while (fscanf(f, "%127s %d %d %d %lf", k, &gr, &gc, &ch, &ms) == 5) {
+        if (key == k && ch <= max_chunk(pl->S)) {
+          fclose(f);
+          if (log) *log = "cached " + key;
+          return ozaki_schedule(pl, gr, gc, ch, err);
+        }
+      }
+      fclose(f);
+    }
+  }
+  ozaki_enqueue(pl, sm_count, s);  // frames and bricks for the timing runs
+  const int shapes[][2] = {{8, 19}, {4, 38}, {16, 9}, {2, 76}, {1, 152}};
+  std::vector<int> chunks{2, 3, max_chunk(pl->S)};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int bgr = pl->tune_gr, bgc = pl->tune_gc, bch = pl->tune_chunk;
+  tagpu_status st = TAGPU_OK;
+  for (const auto& sh : shapes) {
+    for (int ch : chunks) {
+      if (ch > max_chunk(pl->S)) continue;
+      if ((st = ozaki_schedule(pl, sh[0], sh[1], ch, err))) break;
+      float t = 1e30f;
+      for (int rep = 0; rep < 2; ++rep) {
+        cudaEventRecord(e0, s);
+        ozaki_enqueue_gemm(pl, sm_count, s);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        t = std::min(t, ms);
+      }
+      if (t < best) {
+        best = t;
+        bgr = sh[0];
+        bgc = sh[1];
+        bch = ch;
+      }
+    }
+    if (st) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  if ((st = ozaki_schedule(pl, bgr, bgc, bch, err))) return st;
+  if (cache && *cache) {
+    if (FILE* f = fopen(cache, "a")) {
+      fprintf(f, "%s %d %d %d %.4f\n", key.c_str(), bgr, bgc, bch, best);
+      fclose(f);
+    }
+  }
+  if (log) {
+    char buf[256];
+    snprintf(buf, sizeof(buf), "tuned %s: super-tile %dx%d, chunk %d, %.3f ms", key.c_str(), bgr,
+             bgc, bch, best);
+    *log = buf;
+  }
+  return TAGPU_OK;
+}
 
 size_t ozaki_params_size() { return sizeof(OzParams); }
 void ozaki_params(const OzakiPlan* pl, void* out) { *static_cast<OzParams*>(out) = pl->P; }

@@ -937,6 +937,7 @@ struct Contraction {
   tagpu_contract_stats st{};
   OzakiPlan* oz = nullptr;              // emulated form scratch
   size_t oz_bytes = 0;
+  std::string tune_log;
   explicit Contraction(tagpu_ctx* c)
       : ctx(c), d_msz(c), d_nsz(c), d_ksz(c), d_aoff(c), d_boff(c), d_poff(c), d_kidx(c),
         d_coff(c) {}
@@ -1252,18 +1253,26 @@ tagpu_status plan_all(Contraction& c, const char* c_idx, double alpha, tagpu_arr
   if (c.precision == TAGPU_PRECISION_OZAKI && (c.slices < 2 || c.slices > 6))
     return fail(ctx, TAGPU_ERR_INVALID, "slices must be 2..6");
   tagpu_status e;
+  std::string err;
   if ((e = plan_contraction(c, c_idx, alpha, A, a_idx, B, b_idx, cthr))) return e;
   if ((e = run_shape_and_pairs(c))) return e;
   if ((e = make_result(c, A, B))) return e;
   if ((e = prepare_operands(c, A, B))) return e;
   c.view = gemm_view(c);
   if (c.precision == TAGPU_PRECISION_OZAKI && c.npairs > 0 && c.C->elements > 0) {
-    std::string err;
     e = ozaki_plan(ctx->stream, c.view, c.msz.data(), c.nsz.data(), c.ksz.data(), c.slices,
                    &c.oz, &err);
     if (e) return fail(ctx, e, "%s", err.c_str());
     c.oz_bytes = ozaki_scratch_bytes(c.oz);
     ctx->used += c.oz_bytes;
+    const char* env_tune = getenv("TAGPU_AUTOTUNE");
+    if ((opts && opts->autotune) || (env_tune && atoi(env_tune) != 0)) {
+      std::string log;
+      const char* cache = getenv("TAGPU_TUNE_CACHE");
+      e = ozaki_autotune(c.oz, ctx->sm_count, ctx->stream, cache, &log, &err);
+      if (e) return fail(ctx, e, "%s", err.c_str());
+      c.tune_log = log;
+    }
     if (ctx->budget && ctx->used.load() > ctx->budget)
       return fail(ctx, TAGPU_ERR_NOMEM, "emulated-form scratch (%zu bytes) exceeds the budget",
                   c.oz_bytes);
@@ -1517,7 +1526,7 @@ tagpu_status tagpu_batch_add(tagpu_batch* b, const char* c_idx, double alpha, ta
   e.alpha = alpha;
   e.A = A;
   e.B = B;
-  e.opts = opts ? *opts : tagpu_contract_opts{TAGPU_PRECISION_FP64, 0, -1.0f};
+  e.opts = opts ? *opts : tagpu_contract_opts{TAGPU_PRECISION_FP64, 0, -1.0f, 0};
   e.C = new_array(ctx, {});
   b->entries.push_back(std::move(e));
   *c = b->entries.back().C;
@@ -1975,6 +1984,7 @@ tagpu_status tagpu_server_submit(tagpu_server* s, const tagpu_request* req, uint
   r->opts.precision = req->precision >= 0 ? req->precision : s->cfg.precision;
   r->opts.slices = req->slices > 0 ? req->slices : s->cfg.slices;
   r->opts.threshold = -1.0f;
+  r->opts.autotune = 0;
   std::vector<std::string> ai, bi;
   if (!parse_indices(req->a_idx, ai) || !parse_indices(req->b_idx, bi) ||
       (int)ai.size() != req->A->rank || (int)bi.size() != req->B->rank)
