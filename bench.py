@@ -489,14 +489,12 @@ def main():
     barrier()
     clocks = clk.stop()
     total_ms = sum(ms_list)
-    if dist is not None:
-        import torch
-        t = torch.tensor([total_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
     flops = stats["flops"]
-    ms_step = total_ms / args.steps
-    value = flops * ws / (ms_step * 1e-3) / 1e12
+    from tiledarray_gb300.replicas import aggregate
+    job_ms, job_flops, ws = aggregate(total_ms, flops * args.steps, dist,
+                                      f"cuda:{local}" if dist is not None else None)
+    ms_step = job_ms / args.steps
+    value = job_flops / (job_ms * 1e-3) / 1e12
     lat = sorted(ms_list)
     p50 = float(np.percentile(lat, 50))
     p99 = float(np.percentile(lat, 99))
