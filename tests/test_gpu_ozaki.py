@@ -140,6 +140,26 @@ def test_ozaki_batch_graph(ta, world):
     world.check(L.tagpu_batch_destroy(bh))
 
 
+def test_ozaki_accumulator_edge_exact(ta, world):
+    """x = 1 - 2^-8 splits into the extreme leading digits d1 = 128,
+    d2 = -128, so level 2 (d1 e1) and level 3 (d1 e2 + d2 e1) grow by
+    2^14 and 2^15 per k: within their restart periods (32 and 16 stages of
+    32 k) they reach exactly +-2^24, the edge of exact fp32 integer sums.
+    Every digit product is kept, so the result is exact."""
+    x = 1.0 - 2.0 ** -8
+    hm, hk, hn = [0, 128, 200], list(range(0, 4097, 256)), [0, 64, 130]
+    A = ta.DistArray(world, ta.TiledRange([hm, hk]))
+    B = ta.DistArray(world, ta.TiledRange([hk, hn]))
+    nk = len(hk) - 1
+    A.set_tiles({o: np.full((hm[o // nk + 1] - hm[o // nk]) * 256, x) for o in range(2 * nk)})
+    B.set_tiles({o: np.full(256 * (hn[o % 2 + 1] - hn[o % 2]), x if o % 2 == 0 else -x)
+                 for o in range(2 * nk)})
+    C, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI)
+    exp = np.empty((200, 130))
+    exp[:, :64], exp[:, 64:] = 4096 * x * x, -4096 * x * x   # exact in FP64
+    assert np.array_equal(C.to_dense(C.trange), exp)
+
+
 def test_ozaki_row_chunking_identical(ta, world, monkeypatch):
     """A digit bricks built and consumed one range of row blocks at a time
     (forced by a tiny budget) give bit-identical results."""
@@ -165,7 +185,7 @@ def test_ozaki_autotune_identical_and_cached(ta, world, tmp_path, monkeypatch):
                          autotune=True)
     assert np.array_equal(got.download(), ref.download())
     lines = cache.read_text().split("\n")
-    assert lines[0].startswith("S6_") and len(lines[0].split()) == 5
+    assert lines[0].startswith("S6_") and len(lines[0].split()) == 4
     again, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI,
                            autotune=True)
     assert np.array_equal(again.download(), ref.download())

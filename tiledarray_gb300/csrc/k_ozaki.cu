@@ -15,16 +15,20 @@
 //    "bricks" (128 rows x 32 k for A, 64 columns x 32 k for B, in global fused
 //    coordinates) laid out exactly as the K-major no-swizzle UMMA operand image
 //    in shared memory, so one bulk copy moves a brick into place;
-//  * products: for each pair (p, q) with p + q <= S + 1 one
-//    tcgen05.mma.kind::f16 (bf16 x bf16 -> fp32, M=128, N=64, K=16) adds
-//    D_p * E_q into the tensor-memory accumulator of level t = p + q.  Every
-//    product is an integer below 2^14; each chunk of 128 k starts from fresh
-//    accumulators, so a level collects at most (t-1)*128 products and stays
-//    below 6*128*2^14 < 2^24: every fp32 sum is exact integer arithmetic;
-//  * draining: after a chunk the epilogue warps read each level (top level
-//    first, releasing it to the MMA warp at once through a per-level
-//    mbarrier, so the next chunk's MMAs overlap the drain) and fold it into
-//    two exact int64 accumulators per element, hi = L2*2^8 + L3 and
+//  * products: every pair (p, q) with p + q <= S + 1 adds D_p * E_q into the
+//    tensor-memory accumulator of level t = p + q with tcgen05.mma.kind::f16
+//    (bf16 x bf16 -> fp32, M=128, K=16); the levels are adjacent column
+//    ranges and the B slices adjacent in shared memory, so the pairs of one
+//    p form a single MMA of N = 64 * (S + 1 - p) (two above 256).  Every
+//    product is an integer below 2^14.  Level t (t-1 products per k)
+//    restarts from zero every 32/(t-1) stages of 32 k, so levels 2..5 stay
+//    at or below 2^24 where every fp32 sum of integers is exact; levels 6
+//    and 7 (weight 2^-32 and 2^-40 against level 2) sum over the whole
+//    output block in fp32, a rounding below 2^-41 of sum_k |a b|;
+//  * draining: when a level's period ends the epilogue warps read it,
+//    release it to the MMA warp at once through a per-level mbarrier (the
+//    MMAs of the slices that do not touch it never wait), and fold it into
+//    two int64 accumulators per element, hi = L2*2^8 + L3 and
 //    lo = sum_{t>=4} L_t*2^(8(S+1-t));
 //  * recombination (the only FP64 arithmetic): at the end of an output block
 //    C = alpha * 2^(E_A + E_B) * (hi*2^-22 + lo*2^(2-8(S+1))), written into
@@ -53,10 +57,32 @@ namespace {
 constexpr int BM = 128;            // output block rows (MMA M)
 constexpr int BN = 64;             // output block columns (MMA N)
 constexpr int BK = 32;             // k per stage (two MMA K = 16 steps)
-// Fresh accumulators every chunk of `chunk` stages (32 k each).  Exactness
-// bound: level S+1 collects S products of |d e| <= 2^14 per k, so
-// S * 32 * chunk * 2^14 < 2^24, i.e. chunk <= max_chunk(S).
-__host__ __device__ constexpr int max_chunk(int S) { return (1 << 24) / (S * 32 * (1 << 14)); }
+// Level t collects t-1 digit products |d e| <= 2^14 per k.  Levels up to
+// kExactTop are kept exact: level t restarts from zero every
+// drain_period(t) = 32 / (t-1) stages (32 k each), so it never exceeds
+// (t-1) * 32 * drain_period(t) * 2^14 <= 2^24, where every fp32 sum of
+// integers is exact.  Levels above kExactTop (weight 2^-32 and below against
+// level 2) accumulate over the whole output block in fp32 and are read once;
+// their rounding stays below 2^-41 of sum_k |a_ik b_kj| per element, under
+// FP64 GEMM's own worst-case bound.  The schedule is a fixed function of the
+// stage index, so results do not depend on block order or row chunking.
+constexpr int kExactTop = 5;
+__host__ __device__ constexpr int drain_period(int t) { return 32 / (t - 1); }
+// Bit t set: level t (2..TOP) starts from zero at stage x of an output block.
+template <int TOP>
+__device__ __forceinline__ uint32_t restart_mask(int64_t x) {
+  if (x == 0) return ((1u << (TOP + 1)) - 1u) & ~3u;
+  uint32_t m = 0;
+#pragma unroll
+  for (int t = 2; t <= (TOP < kExactTop ? TOP : kExactTop); ++t)
+    if (x % drain_period(t) == 0) m |= 1u << t;
+  return m;
+}
+// Levels read by the epilogue after stage x of an n-stage block.
+template <int TOP>
+__device__ __forceinline__ uint32_t drain_mask(int64_t x, int64_t n) {
+  return x + 1 == n ? restart_mask<TOP>(0) : restart_mask<TOP>(x + 1);
+}
 constexpr int A_SLICE_BYTES = BM * BK * 2;   // 8 KB
 constexpr int B_SLICE_BYTES = BN * BK * 2;   // 4 KB
 constexpr int EPI_WARPS = 8;
@@ -161,9 +187,12 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
   d |= (uint64_t)1 << 46;            // descriptor version for tcgen05
   return d;                          // base offset 0, layout SWIZZLE_NONE
 }
-// kind::f16 instruction descriptor: D f32, A/B bf16, K-major, N=64, M=128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
+// kind::f16 instruction descriptor: D f32, A/B bf16, K-major, M=128, N=n
+// (n a multiple of 16, at most 256).
+__host__ __device__ constexpr uint32_t idesc_n(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(BM >> 4) << 24);
+}
 
 // Correctly rounded double of (hi * 2^sh + lo) * 2^e2 from exact integers
 // (|hi| < 2^61, |lo| < 2^62, 0 <= sh < 64), with integer instructions only;
@@ -245,7 +274,6 @@ struct OzParams {
   double* C;
   int64_t M_total, N_total;
   int* err;                  // error flag (0 = ok)
-  int chunk;                 // stages per accumulation chunk (<= max_chunk(S))
 };
 
 template <int S>
@@ -369,22 +397,62 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
         }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
-    // Chunks of P.chunk stages start from fresh accumulators; before the
-    // first MMA of a chunk into level t, the epilogue must have drained level
-    // t of the previous chunk.  Levels are issued from the top down, the order
-    // in which the epilogue drains them.
+    // Level t lives in tensor-memory columns [(t-2)*BN, (t-1)*BN) and the S
+    // B slices of a stage are contiguous in the K-major image, so the
+    // products of A slice p with B slices for the adjacent levels lo..hi
+    // form ONE MMA of N = (hi-lo+1)*BN (two of half that width above 256).
+    // Slice p feeds the levels p+1..S+1: 8 MMAs of N >= 160, with one of 64,
+    // per k step for S = 6 instead of 21 of N = 64, and far fewer operand
+    // bytes read from shared memory per product.
+    //
+    // A level that restarts at this stage (restart_mask) is zeroed by the
+    // product of slice 1 with slice t-1 alone (accumulate off) once the
+    // epilogue has read it; the slices p >= max restarting level touch no
+    // restarting level and are issued before the wait.  At the first stage
+    // of a block every level restarts; they are read from the top down, so
+    // each level's zeroing product and the slice whose lowest level it is go
+    // out as soon as that level is free.
+    auto mma_levels = [&](uint32_t sb, int p, int ks, int lo, int hi) {
+      const uint32_t a = sb + (p - 1) * A_SLICE_BYTES + ks * 256;
+      const uint32_t b0 = sb + S * A_SLICE_BYTES + (lo - p - 1) * B_SLICE_BYTES + ks * 256;
+      const int n = (hi - lo + 1) * BN;
+      const uint32_t d0 = tmem + (lo - 2) * BN;
+      if (n <= 256) {
+        tc_mma(d0, make_desc(a), make_desc(b0), idesc_n(n), 1u);
+      } else {
+        const int h = n / 2;   // a multiple of 32: B rows start on 8-row groups
+        tc_mma(d0, make_desc(a), make_desc(b0), idesc_n(h), 1u);
+        tc_mma(d0 + h, make_desc(a), make_desc(b0 + (h / 8) * 512), idesc_n(h), 1u);
+      }
+    };
+    auto mma_zero = [&](uint32_t sb, int t) {
+      tc_mma(tmem + (t - 2) * BN, make_desc(sb),
+             make_desc(sb + S * A_SLICE_BYTES + (t - 2) * B_SLICE_BYTES), idesc_n(BN), 0u);
+    };
     int stage = 0;
     uint32_t phase = 0;
-    int64_t chunk = 0;   // chunks issued by this CTA
+    uint32_t level_parity = 0;   // bit t: parity of the next read of level t to wait for
+    uint32_t level_used = 0;     // bit t: level t has been written by this CTA
+    int64_t events = 0;          // acc_full commits
     bool ok = true;
+    auto wait_level = [&](int t) -> bool {
+      if (level_used & (1u << t)) {
+        if (!mbar_wait(smem_u32(&bar_level[t]), (level_parity >> t) & 1u, &abort_s)) {
+          fail(3);
+          return false;
+        }
+        level_parity ^= 1u << t;
+        tc_fence_after();
+      }
+      level_used |= 1u << t;
+      return true;
+    };
     for (int64_t gb = blockIdx.x; gb < nblk_total && ok; gb += gridDim.x) {
       const int vi = find_view(vstart, nviews, gb);
       const OzParams& P = views[vi];
       const int64_t b = gb - vstart[vi];
       const int64_t n = P.blk_rng[2 * b + 1] - P.blk_rng[2 * b];
       for (int64_t x = 0; x < n && ok; ++x) {
-        const bool chunk_start = (x % P.chunk) == 0;
-        const bool chunk_end = ((x + 1) % P.chunk) == 0 || x == n - 1;
         if (!mbar_wait(smem_u32(&bar_full[stage]), phase, &abort_s)) {
           fail(2);
           ok = false;
@@ -392,44 +460,82 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
         }
         tc_fence_after();
         const uint32_t sbase = smem_u32(stage_base + stage * STAGE_BYTES);
+        const uint32_t z = restart_mask<TOP>(x);
+        if (x == 0) {
 #pragma unroll
-        for (int t = TOP; t >= 2; --t) {
-          if (chunk_start && chunk > 0) {
-            if (!mbar_wait(smem_u32(&bar_level[t]), (uint32_t)((chunk - 1) & 1), &abort_s)) {
-              fail(3);
+          for (int t = TOP; t >= 2; --t) {
+            if (!wait_level(t)) {
               ok = false;
               break;
             }
-            tc_fence_after();
+            if (lane == 0) {
+              mma_zero(sbase, t);
+              if (t - 1 >= 2) mma_levels(sbase, t - 1, 0, t, TOP);
+            }
+            __syncwarp();
           }
+          if (!ok) break;
           if (lane == 0) {
 #pragma unroll
-            for (int ks = 0; ks < 2; ++ks) {
+            for (int p = 1; p <= S; ++p) mma_levels(sbase, p, 1, p + 1, TOP);
+          }
+        } else if (z == 0) {
+          if (lane == 0) {
 #pragma unroll
-              for (int p = 1; p < t; ++p) {
-                const int q = t - p;
-                if (p > S || q > S) continue;
-                const uint32_t a = sbase + (p - 1) * A_SLICE_BYTES + ks * 256;
-                const uint32_t bb =
-                    sbase + S * A_SLICE_BYTES + (q - 1) * B_SLICE_BYTES + ks * 256;
-                const uint32_t acc = (chunk_start && ks == 0 && p == 1) ? 0u : 1u;
-                tc_mma(tmem + (t - 2) * BN, make_desc(a), make_desc(bb), kIdesc, acc);
-              }
-            }
+            for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+              for (int p = 1; p <= S; ++p) mma_levels(sbase, p, ks, p + 1, TOP);
+          }
+        } else {
+          const int tmax = 31 - __clz(z);
+          if (lane == 0) {
+#pragma unroll
+            for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+              for (int p = 1; p <= S; ++p)
+                if (p >= tmax) mma_levels(sbase, p, ks, p + 1, TOP);
           }
           __syncwarp();
+#pragma unroll
+          for (int t = TOP; t >= 2; --t)
+            if ((z >> t) & 1u)
+              if (!wait_level(t)) {
+                ok = false;
+                break;
+              }
+          if (!ok) break;
+          if (lane == 0) {
+#pragma unroll
+            for (int t = 2; t <= TOP; ++t)
+              if ((z >> t) & 1u) mma_zero(sbase, t);
+            // slice 1 over the levels that do not restart, in runs
+            int lo = 2;
+#pragma unroll
+            for (int t = 2; t <= TOP + 1; ++t) {
+              if (t == TOP + 1 || ((z >> t) & 1u)) {
+                if (t > lo) mma_levels(sbase, 1, 0, lo, t - 1);
+                lo = t + 1;
+              }
+            }
+#pragma unroll
+            for (int p = 2; p <= S; ++p)
+              if (p < tmax) mma_levels(sbase, p, 0, p + 1, TOP);
+#pragma unroll
+            for (int p = 1; p <= S; ++p)
+              if (p < tmax) mma_levels(sbase, p, 1, p + 1, TOP);
+          }
         }
-        if (!ok) break;
+        __syncwarp();
         if (lane == 0) tc_commit(smem_u32(&bar_empty[stage]));
         __syncwarp();
         if (++stage == STAGES) {
           stage = 0;
           phase ^= 1;
         }
-        if (chunk_end) {
+        if (drain_mask<TOP>(x, n)) {
           if (lane == 0) tc_commit(smem_u32(&bar_acc_full));
           __syncwarp();
-          ++chunk;
+          ++events;
         }
       }
     }
@@ -444,15 +550,16 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
   } else {
     // ------------------------------------------------------------ epilogue
     // Eight warps: warp % 4 selects the 32 tensor-memory lanes (rows) a warp
-    // may access, (warp - 2) / 4 the half of the 64 columns it owns.  Each
-    // chunk's levels are read, released, and folded into two exact int64
+    // may access, (warp - 2) / 4 the half of the 64 columns it owns.  After
+    // each stage that ends a level's period (drain_mask), that level is read,
+    // released to the MMA warp at once, and folded into two int64
     // accumulators per element: hi = L2*2^8 + L3 (unit of level 3) and
     // lo = sum_{t>=4} L_t*2^(8(TOP-t)) (unit of level TOP).
     const int quarter = warp & 3;
     const int half = (warp - 2) >> 2;
     const int rloc = quarter * 32 + lane;
     const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16) + half * 32;
-    int64_t chunk = 0;
+    int64_t events = 0;
     bool ok = true;
     int64_t hi[32], lo[32];
 #pragma unroll
@@ -463,23 +570,34 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
       const int64_t b = gb - vstart[vi];
       const int rb = P.blk[2 * b], cb = P.blk[2 * b + 1];
       const int64_t n = P.blk_rng[2 * b + 1] - P.blk_rng[2 * b];
-      const int64_t nchunks = (n + P.chunk - 1) / P.chunk;
-      for (int64_t c = 0; c < nchunks; ++c, ++chunk) {
-        if (!mbar_wait(smem_u32(&bar_acc_full), (uint32_t)(chunk & 1), &abort_s)) {
+      for (int64_t x = 0; x < n; ++x) {
+        const uint32_t dm = drain_mask<TOP>(x, n);
+        if (!dm) continue;
+        if (!mbar_wait(smem_u32(&bar_acc_full), (uint32_t)(events & 1), &abort_s)) {
           fail(4);
           ok = false;
           break;
         }
+        ++events;
         tc_fence_after();
 #pragma unroll
         for (int t = TOP; t >= 2; --t) {
+          if (!((dm >> t) & 1u)) continue;
           float v0[16], v1[16];
           tmem_ld16(lane_addr + (t - 2) * BN, v0);
           tmem_ld16(lane_addr + (t - 2) * BN + 16, v1);
           tmem_wait_ld();
           tc_fence_before();
           mbar_arrive(smem_u32(&bar_level[t]));
-          if (t >= 4) {
+          if (t > kExactTop) {
+            // whole-block fp32 sum: integer valued, possibly beyond 2^31
+            const int sh = 8 * (TOP - t);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              lo[j] += (int64_t)__float2ll_rn(v0[j]) << sh;
+              lo[16 + j] += (int64_t)__float2ll_rn(v1[j]) << sh;
+            }
+          } else if (t >= 4) {
             const int sh = 8 * (TOP - t);
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
@@ -551,29 +669,35 @@ __device__ __forceinline__ int exp_field(double x) {
   return (int)((__double_as_longlong(x) >> 52) & 0x7ff);
 }
 
-// One warp per (tile, local row): max biased exponent over the row's k.
-__global__ void frame_kernel(OperandView v, const int32_t* __restrict__ row_start,
-                             const int64_t* __restrict__ work, int64_t nwork,
-                             int32_t* __restrict__ E) {
-  const int lane = threadIdx.x & 31;
-  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (w >= nwork) return;
-  // work: tile ordinal (rt*kt_count + kt) << 20 | local row
-  const int64_t packed = work[w];
-  const int64_t t = packed >> 20;
-  const int lr = (int)(packed & 0xfffff);
+// One CTA per operand tile: max biased exponent of each of its rows over the
+// tile's k, folded into the row's frame with atomicMax.  Both storage orders
+// are read coalesced: rows of a row-major tile by warps along k, columns of a
+// transposed tile by threads along the rows.
+__global__ void __launch_bounds__(256) frame_kernel(OperandView v,
+                                                    const int32_t* __restrict__ row_start,
+                                                    int32_t* __restrict__ E) {
+  const int64_t t = blockIdx.x;   // tile (rt, kt), rt-major
   const int64_t rt = t / v.kt, ktile = t - (t / v.kt) * v.kt;
   const int64_t o = v.off[rt * v.off_stride_row + ktile * v.off_stride_k];
   if (o < 0) return;
   const int m = v.rsz[rt], kk = v.ksz[ktile];
   const double* base = v.data + o;
-  int e = 0;
-  for (int k = lane; k < kk; k += 32) {
-    const double x = v.row_contig ? base[(int64_t)k * m + lr] : base[(int64_t)lr * kk + k];
-    e = max(e, exp_field(x));
+  int32_t* Er = E + row_start[rt];
+  if (v.row_contig) {              // element (r, k) at k * m + r
+    for (int r = threadIdx.x; r < m; r += blockDim.x) {
+      int e = 0;
+      for (int k = 0; k < kk; ++k) e = max(e, exp_field(base[(int64_t)k * m + r]));
+      if (e > 0) atomicMax(&Er[r], e);
+    }
+  } else {                         // element (r, k) at r * kk + k
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int r = warp; r < m; r += blockDim.x >> 5) {
+      int e = 0;
+      for (int k = lane; k < kk; k += 32) e = max(e, exp_field(base[(int64_t)r * kk + k]));
+      for (int s = 16; s > 0; s >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, s));
+      if (lane == 0 && e > 0) atomicMax(&Er[r], e);
+    }
   }
-  for (int s = 16; s > 0; s >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, s));
-  if (lane == 0 && e > 0) atomicMax(&E[row_start[rt] + lr], e);
 }
 
 // One CTA per brick: gather ROWS x 32 elements, split into S digit slices,
@@ -798,8 +922,7 @@ struct OzakiPlan {
   int2* blk_ab = nullptr;
   int32_t *EA = nullptr, *EB = nullptr, *brickA = nullptr, *brickB = nullptr, *listA = nullptr,
           *listB = nullptr, *blk = nullptr, *blk_kb = nullptr;
-  int64_t *blk_off = nullptr, *blk_rng = nullptr, *workA = nullptr, *workB = nullptr;
-  int64_t nworkA = 0, nworkB = 0;
+  int64_t *blk_off = nullptr, *blk_rng = nullptr;
   uint8_t *Apack = nullptr, *Bpack = nullptr;
   int* err = nullptr;
   OzParams P{};
@@ -813,9 +936,8 @@ struct OzakiPlan {
   OzParams* d_chunk_params = nullptr;
   int64_t* d_chunk_vstart = nullptr;
   std::vector<int64_t> chunk_rb{0, 0};     // row-block boundaries of the chunks
-  // schedule (results do not depend on it): super-tile of the block order and
-  // stages per accumulation chunk
-  int tune_gr = 8, tune_gc = 19, tune_chunk = 4;
+  // schedule (results do not depend on it): super-tile of the block order
+  int tune_gr = 8, tune_gc = 19;
   std::vector<int32_t> h_blk;              // blocks (rb, cb) in discovery order
   std::vector<int64_t> h_off;              // their k-list offsets
   size_t bytes = 0;
@@ -849,46 +971,57 @@ struct OzakiPlan {
 
 namespace {
 
+constexpr int kMaxDevices = 128;
+
 template <int S>
 void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int64_t nblk,
                    int* err, int sm_count, cudaStream_t st) {
   const size_t smem = Smem<S>::kBytes;
-  static bool set = false;
-  if (!set) {
+  // the shared-memory attribute is per device
+  static bool set[kMaxDevices] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < kMaxDevices && !set[dev]) {
     cudaFuncSetAttribute(ozaki_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
-    set = true;
+    set[dev] = true;
   }
   const int64_t grid = std::min<int64_t>(nblk, sm_count);
-  if (grid > 0)
+  if (grid > 0) {
     ozaki_gemm_kernel<S><<<(unsigned)grid, THREADS, smem, st>>>(views, vstart, nviews, nblk, err);
     count_launch();
+  }
 }
 
 template <int S>
 void launch_split_t(const OzakiPlan& pl, int sm_count, cudaStream_t st, bool do_a, int64_t a0,
                     int64_t a1, bool do_b) {
-  static bool set = false;
-  if (!set) {
+  // the shared-memory attribute is per device
+  static bool set[kMaxDevices] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < kMaxDevices && !set[dev]) {
     cudaFuncSetAttribute(split_kernel<S, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          S * A_SLICE_BYTES);
     cudaFuncSetAttribute(split_kernel<S, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          S * B_SLICE_BYTES);
-    set = true;
+    set[dev] = true;
   }
   const int64_t na = a1 - a0;
   const int grid_a = (int)std::min<int64_t>(na, (int64_t)sm_count * 8);
   const int grid_b = (int)std::min<int64_t>(pl.nB, (int64_t)sm_count * 8);
-  if (do_a && grid_a > 0)
+  if (do_a && grid_a > 0) {
     split_kernel<S, BM><<<grid_a, 256, S * A_SLICE_BYTES, st>>>(
         pl.va, pl.row_tile, pl.row_local, pl.k_tile, pl.k_local, pl.EA, pl.M_total, pl.K_total,
         pl.listA + 2 * a0, na, pl.Apack);
     count_launch();
-  if (do_b && grid_b > 0)
+  }
+  if (do_b && grid_b > 0) {
     split_kernel<S, BN><<<grid_b, 256, S * B_SLICE_BYTES, st>>>(
         pl.vb, pl.col_tile, pl.col_local, pl.k_tile, pl.k_local, pl.EB, pl.N_total, pl.K_total,
         pl.listB, pl.nB, pl.Bpack);
     count_launch();
+  }
 }
 
 void launch_split(const OzakiPlan& pl, int sm_count, cudaStream_t st, bool do_a, int64_t a0,
@@ -918,20 +1051,20 @@ void index_maps(const int32_t* sz, int64_t n, std::vector<int32_t>& tile,
 
 }  // namespace
 
-// Scheduling order of the output blocks and the accumulation chunk length.
+// Scheduling order of the output blocks.
 // Blocks are sorted by row chunk, then by super-tiles of gr row blocks x gc
 // column blocks (with 152 CTAs, 8 x 19 is one wave), so CTAs running together
 // share A bricks (gc ways) and B bricks (gr ways) in L2.  Results do not
-// depend on the schedule: every sum is exact.
-tagpu_status ozaki_schedule(OzakiPlan* pl, int gr, int gc, int chunk, std::string* err) {
-  if (gr < 1 || gc < 1 || chunk < 1 || chunk > max_chunk(pl->S)) {
+// depend on the schedule: the order of every block's sums is fixed by its
+// own k blocks.
+tagpu_status ozaki_schedule(OzakiPlan* pl, int gr, int gc, std::string* err) {
+  if (gr < 1 || gc < 1) {
     *err = "bad emulated-form schedule";
     return TAGPU_ERR_INVALID;
   }
   cudaStream_t s = pl->s;
   pl->tune_gr = gr;
   pl->tune_gc = gc;
-  pl->tune_chunk = chunk;
   const auto& hb = pl->h_blk;
   const auto& ho = pl->h_off;
   const int64_t nsc = (pl->CB + gc - 1) / gc;
@@ -964,7 +1097,6 @@ tagpu_status ozaki_schedule(OzakiPlan* pl, int gr, int gc, int chunk, std::strin
     cudaMemcpyAsync(pl->blk_rng, rng.data(), rng.size() * 8, cudaMemcpyHostToDevice, s);
   }
   // the slot pairs follow the k lists, which did not move
-  pl->P.chunk = chunk;
   if (pl->nchunk > 1) {
     std::vector<OzParams> cp(pl->nchunk, pl->P);
     std::vector<int64_t> cv(2 * pl->nchunk);
@@ -1051,23 +1183,6 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   b.rsz = v.nsz;
   b.ksz = v.ksz;
   b.row_contig = v.b_trans ? 0 : 1;  // k x n storage: rows (n) contiguous
-  // frame work lists (tile, local row) on the host from the offsets
-  std::vector<int64_t> aoff_h(v.Mt * v.Kt), boff_h(v.Kt * v.Nt);
-  cudaMemcpyAsync(aoff_h.data(), v.aoff, aoff_h.size() * 8, cudaMemcpyDeviceToHost, s);
-  cudaMemcpyAsync(boff_h.data(), v.boff, boff_h.size() * 8, cudaMemcpyDeviceToHost, s);
-  cudaStreamSynchronize(s);
-  std::vector<int64_t> wa, wb;
-  for (int64_t i = 0; i < v.Mt; ++i)
-    for (int64_t k = 0; k < v.Kt; ++k)
-      if (aoff_h[i * v.Kt + k] >= 0)
-        for (int32_t r = 0; r < h_msz[i]; ++r) wa.push_back(((i * v.Kt + k) << 20) | r);
-  for (int64_t j = 0; j < v.Nt; ++j)
-    for (int64_t k = 0; k < v.Kt; ++k)
-      if (boff_h[k * v.Nt + j] >= 0)
-        for (int32_t r = 0; r < h_nsz[j]; ++r) wb.push_back(((j * v.Kt + k) << 20) | r);
-  pl->nworkA = (int64_t)wa.size();
-  pl->nworkB = (int64_t)wb.size();
-  if ((st = pl->upload(&pl->workA, wa, err)) || (st = pl->upload(&pl->workB, wb, err))) return st;
   // brick maps
   int64_t* flag = nullptr;
   int64_t* scan = nullptr;
@@ -1139,11 +1254,12 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
                                                              pl->blk_off);
   count_launch();
   if ((st = pl->alloc(&pl->blk_ab, pl->nkb, err))) return st;
-  if (pl->nblk)
+  if (pl->nblk) {
     slot_pairs_kernel<<<blocks_for(pl->nblk * 32, 256), 256, 0, s>>>(
         pl->blk, pl->blk_off, pl->nblk, pl->blk_kb, pl->brickA, pl->brickB, pl->KB, pl->CB,
         pl->blk_ab);
     count_launch();
+  }
   // Row chunking: when the A bricks would not fit next to everything else,
   // they are built and consumed one range of row blocks at a time.
   const size_t a_brick = (size_t)slices * A_SLICE_BYTES, b_brick = (size_t)slices * B_SLICE_BYTES;
@@ -1183,7 +1299,6 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
     cudaStreamSynchronize(s);
   }
   if ((st = pl->alloc(&pl->blk_rng, 2 * pl->nblk, err))) return st;
-  pl->tune_chunk = std::min(4, max_chunk(slices));
   // operand slices (A: the largest chunk)
   int64_t max_slots = 0;
   for (int c = 0; c < pl->nchunk; ++c)
@@ -1227,7 +1342,7 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
     return st;
   if ((st = pl->alloc(&pl->d_params, 1, err)) || (st = pl->alloc(&pl->d_vstart, 2, err)))
     return st;
-  if ((st = ozaki_schedule(pl.get(), pl->tune_gr, pl->tune_gc, pl->tune_chunk, err))) return st;
+  if ((st = ozaki_schedule(pl.get(), pl->tune_gr, pl->tune_gc, err))) return st;
   *out = pl.release();
   return TAGPU_OK;
 }
@@ -1237,14 +1352,15 @@ void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s) {
   cudaMemsetAsync(pl->EA, 0, pl->M_total * 4, s);
   cudaMemsetAsync(pl->EB, 0, pl->N_total * 4, s);
   cudaMemsetAsync(pl->err, 0, 4, s);
-  if (pl->nworkA)
-    frame_kernel<<<blocks_for(pl->nworkA * 32, 256), 256, 0, s>>>(pl->va, pl->rstart, pl->workA,
-                                                                   pl->nworkA, pl->EA);
+  const int64_t ta = pl->va.rowt * pl->va.kt, tb = pl->vb.rowt * pl->vb.kt;
+  if (ta > 0) {
+    frame_kernel<<<(unsigned)ta, 256, 0, s>>>(pl->va, pl->rstart, pl->EA);
     count_launch();
-  if (pl->nworkB)
-    frame_kernel<<<blocks_for(pl->nworkB * 32, 256), 256, 0, s>>>(pl->vb, pl->cstart, pl->workB,
-                                                                   pl->nworkB, pl->EB);
+  }
+  if (tb > 0) {
+    frame_kernel<<<(unsigned)tb, 256, 0, s>>>(pl->vb, pl->cstart, pl->EB);
     count_launch();
+  }
   // chunked plans split A chunk by chunk inside ozaki_enqueue_gemm
   launch_split(*pl, sm_count, s, pl->nchunk == 1, 0, pl->nA, true);
 }
@@ -1301,14 +1417,15 @@ tagpu_status ozaki_autotune(OzakiPlan* pl, int sm_count, cudaStream_t s, const c
   const std::string key = tune_bucket(pl);
   if (cache && *cache) {
     if (FILE* f = fopen(cache, "r")) {
-      char k[128];
-      int gr, gc, ch;
-      double ms;
-      while (fscanf(f, "%127s %d %d %d %lf", k, &gr, &gc, &ch, &ms) == 5) {
-        if (key == k && ch <= max_chunk(pl->S)) {
+      char line[256];
+      while (fgets(line, sizeof(line), f)) {
+        char k[128], extra[8];
+        int gr, gc;
+        double ms;
+        if (sscanf(line, "%127s %d %d %lf %7s", k, &gr, &gc, &ms, extra) == 4 && key == k) {
           fclose(f);
           if (log) *log = "cached " + key;
-          return ozaki_schedule(pl, gr, gc, ch, err);
+          return ozaki_schedule(pl, gr, gc, err);
         }
       }
       fclose(f);
@@ -1316,50 +1433,44 @@ tagpu_status ozaki_autotune(OzakiPlan* pl, int sm_count, cudaStream_t s, const c
   }
   ozaki_enqueue(pl, sm_count, s);  // frames and bricks for the timing runs
   const int shapes[][2] = {{8, 19}, {4, 38}, {16, 9}, {2, 76}, {1, 152}};
-  std::vector<int> chunks{2, 3, max_chunk(pl->S)};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  int bgr = pl->tune_gr, bgc = pl->tune_gc, bch = pl->tune_chunk;
+  int bgr = pl->tune_gr, bgc = pl->tune_gc;
   tagpu_status st = TAGPU_OK;
   for (const auto& sh : shapes) {
-    for (int ch : chunks) {
-      if (ch > max_chunk(pl->S)) continue;
-      if ((st = ozaki_schedule(pl, sh[0], sh[1], ch, err))) break;
-      float t = 1e30f;
-      for (int rep = 0; rep < 2; ++rep) {
-        cudaEventRecord(e0, s);
-        ozaki_enqueue_gemm(pl, sm_count, s);
-        cudaEventRecord(e1, s);
-        cudaEventSynchronize(e1);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        t = std::min(t, ms);
-      }
-      if (t < best) {
-        best = t;
-        bgr = sh[0];
-        bgc = sh[1];
-        bch = ch;
-      }
+    if ((st = ozaki_schedule(pl, sh[0], sh[1], err))) break;
+    float t = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {
+      cudaEventRecord(e0, s);
+      ozaki_enqueue_gemm(pl, sm_count, s);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      t = std::min(t, ms);
     }
-    if (st) break;
+    if (t < best) {
+      best = t;
+      bgr = sh[0];
+      bgc = sh[1];
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st) return st;
-  if ((st = ozaki_schedule(pl, bgr, bgc, bch, err))) return st;
+  if ((st = ozaki_schedule(pl, bgr, bgc, err))) return st;
   if (cache && *cache) {
     if (FILE* f = fopen(cache, "a")) {
-      fprintf(f, "%s %d %d %d %.4f\n", key.c_str(), bgr, bgc, bch, best);
+      fprintf(f, "%s %d %d %.4f\n", key.c_str(), bgr, bgc, best);
       fclose(f);
     }
   }
   if (log) {
     char buf[256];
-    snprintf(buf, sizeof(buf), "tuned %s: super-tile %dx%d, chunk %d, %.3f ms", key.c_str(), bgr,
-             bgc, bch, best);
+    snprintf(buf, sizeof(buf), "tuned %s: super-tile %dx%d, %.3f ms", key.c_str(), bgr, bgc,
+             best);
     *log = buf;
   }
   return TAGPU_OK;
