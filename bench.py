@@ -239,6 +239,38 @@ def _line(args, metric, value, unit, ms, cfg, extra):
     print(json.dumps(out), flush=True)
 
 
+def ccsd_spot_check(C, V, T, hv, ho, thr, count=2):
+    """Result tiles R(a,b,i,j) recomputed on the CPU in numpy FP64 from the
+    operand tiles fetched from the device: the sum over the (c,d) tiles present
+    in both shapes of V(a,b,c,d) @ T(c,d,i,j).  Checks the emulated GEMM at
+    sizes where the plain FP64 form would take minutes per step.  Returns the
+    largest relative Frobenius error over the checked tiles (the smallest v
+    tiles, so the check stays at a few seconds at v = 384)."""
+    nv, no = len(hv) - 1, len(ho) - 1
+    sv, so = np.diff(np.asarray(hv)), np.diff(np.asarray(ho))
+    voff, toff, coff = V.tile_offsets(), T.tile_offsets(), C.tile_offsets()
+    order = np.argsort(sv, kind="stable")
+    a0, a1 = int(order[0]), int(order[min(1, nv - 1)])
+    picks = [(a0, a1, 0, no - 1), (a1, a0, no - 1, 0)][:count]
+    worst, checked = 0.0, 0
+    for a, b, i, j in picks:
+        o = ((a * nv + b) * no + i) * no + j
+        if coff[o] < 0:
+            continue
+        acc = np.zeros((sv[a] * sv[b], so[i] * so[j]))
+        for c in range(nv):
+            for d in range(nv):
+                ov = ((a * nv + b) * nv + c) * nv + d
+                ot = ((c * nv + d) * no + i) * no + j
+                if voff[ov] < 0 or toff[ot] < 0:
+                    continue
+                acc += V.tile(ov, (acc.shape[0], -1)) @ T.tile(ot, (-1, acc.shape[1]))
+        got = C.tile(o, acc.shape)
+        worst = max(worst, float(np.linalg.norm(got - acc) / max(np.linalg.norm(acc), 1e-300)))
+        checked += 1
+    return worst, checked
+
+
 def run_secondary(args):
     """The other configurations: measured lines for the record, not the
     headline (the default run is the block-sparse N=16384 product)."""
@@ -285,23 +317,43 @@ def run_secondary(args):
         thr = 1e-8
         w.threshold = thr
         V = ta.DistArray(w, ta.TiledRange([hv, hv, hv, hv]))
-        T = ta.DistArray(w, ta.TiledRange([hv, hv, ho, ho]))
         V.generate(args.seed, 0, 0, vs, True, thr)
-        T.generate(args.seed, 1, 0, ts, True, thr)
+        # identity: V(a,b,c,d) T(c,d,i,j); transpose: T stored as (i,j,c,d), the
+        # form of the reference's abcd example, folded into the GEMM loaders;
+        # general: V read as (a,c,b,d), an explicit tile permutation into GEMM order
+        if args.form == "transpose":
+            T = ta.DistArray(w, ta.TiledRange([ho, ho, hv, hv]))
+            T.generate(args.seed, 1, 0, np.ascontiguousarray(ts.transpose(2, 3, 0, 1)), True, thr)
+            a_idx, b_idx = "a,b,c,d", "i,j,c,d"
+        else:
+            T = ta.DistArray(w, ta.TiledRange([hv, hv, ho, ho]))
+            T.generate(args.seed, 1, 0, ts, True, thr)
+            a_idx, b_idx = ("a,c,b,d" if args.form == "general" else "a,b,c,d"), "c,d,i,j"
         res = {}
         ms = timed(lambda: res.__setitem__("c", ta.contract(
-            w, "a,b,i,j", 1.0, V, "a,b,c,d", T, "c,d,i,j", precision=prec)),
+            w, "a,b,i,j", 1.0, V, a_idx, T, b_idx, precision=prec)),
             args.steps, args.warmup)
         C, st = res["c"]
-        extra = {"phases_ms": {k: st[k] for k in ("ms_shape", "ms_pairs", "ms_split", "ms_gemm")},
-                 "pairs": st["pairs"], "flops_per_step": st["flops"]}
+        extra = {"phases_ms": {k: st[k] for k in ("ms_shape", "ms_pairs", "ms_permute",
+                                                  "ms_split", "ms_gemm")},
+                 "pairs": st["pairs"], "flops_per_step": st["flops"],
+                 "permtypes": [st["left_permtype"], st["right_permtype"]]}
+        if st["left_permtype"] == 3 and st["ms_permute"] > 0:
+            moved = 16.0 * V.info().elements
+            extra["permute"] = {"bytes": moved, "GB_per_s": moved / st["ms_permute"] / 1e6,
+                                "hbm_peak_GB_per_s": peaks()[0]}
         if not args.no_plain and prec == ta.PRECISION_OZAKI:
-            err, stp = err_vs_plain(C, "a,b,i,j", V, "a,b,c,d", T, "c,d,i,j")
+            err, stp = err_vs_plain(C, "a,b,i,j", V, a_idx, T, b_idx)
             extra.update({"rel_err_vs_plain_fp64": err, "plain_fp64_tflops":
                           st["flops"] / stp["ms_total"] / 1e9})
+        if not args.no_cpu and args.form == "identity":
+            t0 = time.perf_counter()
+            err, nchk = ccsd_spot_check(C, V, T, hv, ho, thr)
+            extra["spot_check_vs_cpu"] = {"tiles": nchk, "max_rel_err": err,
+                                          "seconds": time.perf_counter() - t0}
         m = statistics.median(ms)
         _line(args, "ccsd-like 4-index nonzero-block TFLOP/s", st["flops"] / m / 1e9, "TFLOP/s",
-              m, {"workload": f"R(a,b,i,j)=V(a,b,c,d)*T(c,d,i,j) o=48 v={args.v}",
+              m, {"workload": f"R(a,b,i,j)=V({a_idx})*T({b_idx}) o=48 v={args.v}",
                   "precision": args.precision, "V_bytes": V.info().device_bytes}, extra)
     elif args.workload == "batched":
         import ctypes
@@ -313,30 +365,44 @@ def run_secondary(args):
             A.generate(args.seed, 2 * x, 0, ka, True)
             B.generate(args.seed, 2 * x + 1, 0, kb, True)
             ops.append((A, B))
-        bh = ctypes.c_void_p()
-        w.check(w.L.tagpu_batch_create(w.h, ctypes.byref(bh)))
-        outs = []
-        opts = ta.ContractOpts(prec, args.slices, -1.0)
-        for A, B in ops:
-            ch = ctypes.c_void_p()
-            w.check(w.L.tagpu_batch_add(bh, b"i,j,l", 1.0, A.h, b"i,j,k", B.h, b"k,l",
-                                        ctypes.byref(opts), ctypes.byref(ch)))
-            outs.append(ta.DistArray(w, _handle=ch))
-        t0 = time.perf_counter()
-        w.check(w.L.tagpu_batch_run(bh))   # plan + capture + first run
-        plan_s = time.perf_counter() - t0
-        bst = ta.ContractStats()
-        w.check(w.L.tagpu_batch_stats(bh, ctypes.byref(bst)))
-        ms = timed(lambda: w.check(w.L.tagpu_batch_run(bh)), args.steps, args.warmup)
+        def batch(precision, steps, warmup):
+            bh = ctypes.c_void_p()
+            w.check(w.L.tagpu_batch_create(w.h, ctypes.byref(bh)))
+            outs = []
+            opts = ta.ContractOpts(precision, args.slices, -1.0)
+            for A, B in ops:
+                ch = ctypes.c_void_p()
+                w.check(w.L.tagpu_batch_add(bh, b"i,j,l", 1.0, A.h, b"i,j,k", B.h, b"k,l",
+                                            ctypes.byref(opts), ctypes.byref(ch)))
+                outs.append(ta.DistArray(w, _handle=ch))
+            t0 = time.perf_counter()
+            w.check(w.L.tagpu_batch_run(bh))   # plan + capture + first run
+            plan_s = time.perf_counter() - t0
+            bst = ta.ContractStats()
+            w.check(w.L.tagpu_batch_stats(bh, ctypes.byref(bst)))
+            ms = timed(lambda: w.check(w.L.tagpu_batch_run(bh)), steps, warmup)
+            w.check(w.L.tagpu_batch_destroy(bh))
+            return ms, bst, plan_s, outs
+
+        ms, bst, plan_s, outs = batch(prec, args.steps, args.warmup)
         m = statistics.median(ms)
-        w.check(w.L.tagpu_batch_destroy(bh))
+        extra = {"flops_per_step": bst.flops, "pairs": bst.pairs, "plan_and_capture_s": plan_s,
+                 "latency_ms": {"p50": float(np.percentile(ms, 50)),
+                                "p99": float(np.percentile(ms, 99))}}
+        if not args.no_plain and prec == ta.PRECISION_OZAKI:
+            pms, _, _, pouts = batch(ta.PRECISION_FP64, 1, 1)
+            x = np.concatenate([o.download() for o in outs])
+            y = np.concatenate([o.download() for o in pouts])
+            pm = statistics.median(pms)
+            extra.update({"plain_fp64": {"value": bst.flops / pm / 1e9, "ms_per_step": pm,
+                                         "unit": "TFLOP/s"},
+                          "emulated_over_plain": pm / m,
+                          "rel_err_vs_plain_fp64": float(np.linalg.norm(x - y) /
+                                                         max(np.linalg.norm(y), 1e-300))})
         _line(args, "batched nonzero-block TFLOP/s (one graph replay per step)",
               bst.flops / m / 1e9, "TFLOP/s", m,
               {"workload": f"{args.count} x C(i,j,l)=A(i,j,k)*B(k,l), extents log-U[32,512], "
-                           "tiles U[32,128], 30% dropout", "precision": args.precision},
-              {"flops_per_step": bst.flops, "pairs": bst.pairs, "plan_and_capture_s": plan_s,
-               "latency_ms": {"p50": float(np.percentile(ms, 50)),
-                              "p99": float(np.percentile(ms, 99))}})
+                           "tiles U[32,128], 30% dropout", "precision": args.precision}, extra)
     elif args.workload == "serve":
         run_serve(args, w, ta, wl, prec)
     w.close()
@@ -431,6 +497,8 @@ def main():
     ap.add_argument("--workload", default="blocksparse",
                     choices=["blocksparse", "dense", "ccsd", "batched", "serve"])
     ap.add_argument("--v", type=int, default=192, help="ccsd: virtual extent")
+    ap.add_argument("--form", default="identity", choices=["identity", "transpose", "general"],
+                    help="ccsd: operand index order (general = explicit tile permutation)")
     ap.add_argument("--count", type=int, default=512, help="batched: contractions")
     ap.add_argument("--requests", type=int, default=300, help="serve: requests")
     ap.add_argument("--rate", type=float, default=40.0, help="serve: Poisson arrivals / s")

@@ -131,6 +131,13 @@ tagpu_status tagpu_array_generate(tagpu_array* a, uint64_t seed, uint64_t stream
                                   int kind, const double* tile_scale,
                                   int compute_shape, float threshold);
 
+/* TiledArray::truncate (conversions/truncate.h:52-80): the shape is rebuilt
+ * from the Frobenius norms of the stored tiles (computed on the device in
+ * storage order, as Tensor::norm), scaled by tile volume, with `threshold`
+ * (negative: the context default); tiles below it are dropped and the rest
+ * compacted in place.  Zero tiles stay zero.  A dense array is left as is. */
+tagpu_status tagpu_array_truncate(tagpu_array* a, float threshold);
+
 typedef struct tagpu_array_info {
   int rank;
   int dense;                  /* 1: DensePolicy */
@@ -147,6 +154,11 @@ tagpu_status tagpu_array_get_info(const tagpu_array* a, tagpu_array_info* info);
 tagpu_status tagpu_array_get_norms(const tagpu_array* a, float* norms);
 /* Element offset of every tile in the upload/download buffer, -1 if zero. */
 tagpu_status tagpu_array_get_tile_offsets(const tagpu_array* a, int64_t* offsets);
+/* One tile to the host: `DistArray::find(i).get()` (dist_array.h:717-733)
+ * for tile ordinal `ordinal` (row-major over the tile grid); n must equal the
+ * tile's volume.  A zero tile is TAGPU_ERR_INVALID. */
+tagpu_status tagpu_array_get_tile(const tagpu_array* a, int64_t ordinal, double* tile,
+                                  int64_t n);
 /* Tiling of the array: hashmarks of dimension d (ntiles[d]+1 values). */
 tagpu_status tagpu_array_get_hashmarks(const tagpu_array* a, int d,
                                        int64_t* hashmarks);
@@ -192,6 +204,19 @@ tagpu_status tagpu_contract(tagpu_ctx* ctx, const char* c_idx, double alpha,
                             const char* b_idx, const tagpu_contract_opts* opts,
                             tagpu_array** c);
 tagpu_status tagpu_last_stats(const tagpu_ctx* ctx, tagpu_contract_stats* st);
+
+/* c += alpha * A(a_idx) * B(b_idx): `C("i,j") += A("i,k") * B("k,j")`
+ * (expressions/tsr_expr.h:146-152, an AddExpr of the target and the
+ * product).  The product is formed as by tagpu_contract in the target's index
+ * order and must have the target's tiling; the new shape is SparseShape::add
+ * (sparse_shape.h:1309-1328): float sum of the two scaled norms, zero below
+ * the context threshold.  Tiles present in both are summed with one rounding,
+ * a tile present in one is copied.  Dense and sparse policies do not mix.
+ * Statistics of the product are in tagpu_last_stats. */
+tagpu_status tagpu_contract_accumulate(tagpu_ctx* ctx, const char* c_idx, double alpha,
+                                       tagpu_array* A, const char* a_idx, tagpu_array* B,
+                                       const char* b_idx, const tagpu_contract_opts* opts,
+                                       tagpu_array* C);
 
 /* ---- single steps, host buffers (for parity tests) ----------------------- */
 /* Kernel (a): result[M x N] = |factor| * (left[M x K] * k_sizes) x

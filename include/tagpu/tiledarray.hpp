@@ -140,6 +140,8 @@ struct TsrExpr {
   std::string idx;
   double factor;
   TsrExpr& operator=(const struct MultExpr& e);
+  // C("i,j") += A("i,k") * B("k,j") (expressions/tsr_expr.h:146-152)
+  TsrExpr& operator+=(const struct MultExpr& e);
 };
 
 struct MultExpr {
@@ -252,6 +254,16 @@ inline TsrExpr& TsrExpr::operator=(const MultExpr& e) {
                          e.left.idx.c_str(), e.right.array->handle(), e.right.idx.c_str(), &o,
                          &c));
   array->reset(c, &w);
+  return *this;
+}
+
+inline TsrExpr& TsrExpr::operator+=(const MultExpr& e) {
+  World& w = e.left.array->world();
+  tagpu_contract_opts o = array->opts();
+  w.check(tagpu_contract_accumulate(w.ctx(), idx.c_str(), e.factor * factor,
+                                    e.left.array->handle(), e.left.idx.c_str(),
+                                    e.right.array->handle(), e.right.idx.c_str(), &o,
+                                    array->handle()));
   return *this;
 }
 

@@ -70,6 +70,11 @@ int main() {
   E.set_precision(TAGPU_PRECISION_OZAKI);
   E("i,j") = A("i,k") * B("k,j");
   fails += check("emulated C(i,j)", dense(E, {{0, 3, 7}, {0, 4, 6}}), ref);
+  // accumulate: C already holds A*B, so C += 0.5 * A*B gives 1.5 * A*B
+  C("i,j") += 0.5 * (A("i,k") * B("k,j"));
+  std::vector<double> ref15(ref);
+  for (auto& v : ref15) v *= 1.5;
+  fails += check("C(i,j) += 0.5 * A(i,k) * B(k,j)", dense(C, {{0, 3, 7}, {0, 4, 6}}), ref15);
   C = TA::TSpArrayD();
   D = TA::TSpArrayD();
   E = TA::TSpArrayD();

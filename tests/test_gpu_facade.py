@@ -28,4 +28,4 @@ def test_facade_runs(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     print(r.stdout, r.stderr)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert r.stdout.count("ok ") == 3
+    assert r.stdout.count("ok ") == 4

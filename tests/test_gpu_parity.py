@@ -217,3 +217,79 @@ def test_all_screened_result(ta, world):
 def test_fp64_rates_measured(ta, world):
     dmma, dfma = world.fp64_rates()
     assert 0.05 < dmma < 200 and 0.05 < dfma < 200
+
+
+def test_get_tile_matches_download(ta, world):
+    h = uneven_hashmarks(300, 20, 90, 8)
+    keep = (np.arange((len(h) - 1) ** 2) % 4) != 1
+    A, tr = gpu_operand(ta, world, [h, h], 4, 0, kind=0, keep=keep)
+    full, offs = A.download(), A.tile_offsets()
+    for o in np.flatnonzero(offs >= 0):
+        t = A.tile(int(o))
+        assert np.array_equal(t.ravel(), full[offs[o]:offs[o] + t.size])
+    zero = int(np.flatnonzero(offs < 0)[0])
+    with pytest.raises(ta.TAGPUError):
+        A.tile(zero)
+
+
+def test_truncate_matches_make_array(oracle, ta, world):
+    """truncate with a larger threshold equals building the array with that
+    threshold from the start (make_array semantics): same scaled norms, same
+    surviving tiles, zero tiles stay zero."""
+    h = uneven_hashmarks(600, 40, 120, 12)
+    nt = len(h) - 1
+    I, J = np.meshgrid(np.arange(nt), np.arange(nt), indexing="ij")
+    scale = np.exp(-np.abs(I - J) * 3.0)
+    keep = (np.arange(nt * nt) % 5) != 2
+    A, tr = gpu_operand(ta, world, [h, h], 6, 0, kind=0, keep=keep, tile_scale=scale,
+                        threshold=1e-14)
+    A.truncate(1e-6)
+    Ao = oracle_operand(oracle, [h, h], 6, 0, kind=0, keep=keep, tile_scale=scale,
+                        threshold=1e-6)
+    assert np.array_equal(A.norms(), Ao.norms.ravel())
+    got = A.tiles(tr)
+    assert set(got) == set(Ao.tiles) and len(got) < int(keep.sum())
+    for o, t in Ao.tiles.items():
+        assert np.array_equal(got[o], t)
+    info = A.info()
+    assert info.zero_tiles == nt * nt - len(got)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_contract_accumulate(ta, world, precision):
+    """C("i,j") += alpha * A2("i,k") * B2("k,j"): the shape is the float sum of
+    the two scaled norms, zero below the threshold (SparseShape::add); tiles in
+    both are summed with one rounding, tiles in one are copied."""
+    h = uneven_hashmarks(700, 40, 140, 14)
+    nt = len(h) - 1
+    I, J = np.meshgrid(np.arange(nt), np.arange(nt), indexing="ij")
+    band = lambda w0: np.where(np.abs(I - J) <= w0, 1.0, 0.0)
+    thr = 1e-8
+    world.threshold = thr
+    try:
+        A, _ = gpu_operand(ta, world, [h, h], 21, 0, kind=0, tile_scale=band(1), threshold=thr)
+        B, _ = gpu_operand(ta, world, [h, h], 21, 1, kind=0, tile_scale=band(1), threshold=thr)
+        A2, _ = gpu_operand(ta, world, [h, h], 22, 0, kind=0, tile_scale=band(2) * (I >= J),
+                            threshold=thr)
+        B2, _ = gpu_operand(ta, world, [h, h], 22, 1, kind=0, tile_scale=band(2), threshold=thr)
+        C, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=precision)
+        P, _ = ta.contract(world, "i,j", -0.75, A2, "i,k", B2, "k,j", precision=precision)
+        c_n, c_off, c_d = C.norms(), C.tile_offsets(), C.download()
+        p_n, p_off, p_d = P.norms(), P.tile_offsets(), P.download()
+        ta.contract_accumulate(world, C, "i,j", -0.75, A2, "i,k", B2, "k,j", precision=precision)
+    finally:
+        world.threshold = ta.FLT_EPSILON
+    exp_n = (c_n + p_n).astype(np.float32)
+    exp_n[exp_n < np.float32(thr)] = 0
+    assert np.array_equal(C.norms(), exp_n)
+    assert (p_off >= 0).sum() > 0 and ((c_off < 0) & (p_off >= 0)).sum() > 0
+    r_off, r_d = C.tile_offsets(), C.download()
+    tr = C.trange
+    for t in np.flatnonzero(r_off >= 0):
+        i, j = divmod(int(t), nt)
+        vol = (h[i + 1] - h[i]) * (h[j + 1] - h[j])
+        c = c_d[c_off[t]:c_off[t] + vol] if c_off[t] >= 0 else None
+        p = p_d[p_off[t]:p_off[t] + vol] if p_off[t] >= 0 else None
+        want = c + p if (c is not None and p is not None) else (c if c is not None else p)
+        assert np.array_equal(r_d[r_off[t]:r_off[t] + vol], want)
+    assert set(np.flatnonzero(r_off >= 0)) == set(np.flatnonzero(exp_n > 0))

@@ -135,6 +135,11 @@ SIGNATURES = {
     "tagpu_array_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(ArrayInfo)]),
     "tagpu_array_get_norms": (ctypes.c_int, [_vp, _f32p]),
     "tagpu_array_get_tile_offsets": (ctypes.c_int, [_vp, _i64p]),
+    "tagpu_array_get_tile": (ctypes.c_int, [_vp, ctypes.c_int64, _f64p, ctypes.c_int64]),
+    "tagpu_array_truncate": (ctypes.c_int, [_vp, ctypes.c_float]),
+    "tagpu_contract_accumulate": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, _vp,
+                                                 ctypes.c_char_p, _vp, ctypes.c_char_p, _vp,
+                                                 _vp]),
     "tagpu_array_get_hashmarks": (ctypes.c_int, [_vp, ctypes.c_int, _i64p]),
     "tagpu_contract": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, _vp,
                                       ctypes.c_char_p, _vp, ctypes.c_char_p,
@@ -330,6 +335,19 @@ class TsrExpr:
     def __init__(self, array, indices, factor=1.0):
         self.array, self.indices, self.factor = array, indices, factor
 
+    def __iadd__(self, expr):
+        """C("i,j") += A("i,k") * B("k,j") (TsrExpr::operator+=)."""
+        if not isinstance(expr, MultExpr):
+            raise TypeError("only contractions A(...) * B(...) are on this path")
+        a = self.array
+        opts = ContractOpts(a.precision, a.slices, -1.0, 0)
+        W = a.world
+        W.check(W.L.tagpu_contract_accumulate(
+            W.h, self.indices.encode(), float(expr.factor), expr.left.array.h,
+            expr.left.indices.encode(), expr.right.array.h, expr.right.indices.encode(),
+            ctypes.byref(opts), a.h))
+        return _Accumulated(self)
+
     def __mul__(self, other):
         if isinstance(other, TsrExpr):
             return MultExpr(self, other, self.factor * other.factor)
@@ -337,6 +355,13 @@ class TsrExpr:
 
     def __rmul__(self, s):
         return TsrExpr(self.array, self.indices, self.factor * float(s))
+
+
+class _Accumulated:
+    """Result of `+=` on a TsrExpr: the target already holds the sum."""
+
+    def __init__(self, target):
+        self.target = target
 
 
 class MultExpr:
@@ -416,6 +441,21 @@ class DistArray:
         self.world.check(self.world.L.tagpu_array_get_tile_offsets(self.h, _p(out, _i64p)))
         return out
 
+    def tile(self, ordinal: int, shape=None):
+        """One nonzero tile (DistArray::find(i).get()), reshaped to `shape`."""
+        tr = self.trange
+        idx, o = [], int(ordinal)
+        for d in reversed(range(len(tr.dims))):
+            n = len(tr.dims[d]) - 1
+            idx.append(o % n)
+            o //= n
+        idx.reverse()
+        ext = tuple(tr.dims[d][x + 1] - tr.dims[d][x] for d, x in enumerate(idx))
+        out = np.empty(max(1, int(np.prod(ext))), np.float64)
+        self.world.check(self.world.L.tagpu_array_get_tile(self.h, int(ordinal), _p(out, _f64p),
+                                                           int(np.prod(ext))))
+        return out[:int(np.prod(ext))].reshape(shape if shape is not None else ext)
+
     def upload(self, packed):
         packed = np.ascontiguousarray(packed, np.float64)
         self.world.check(self.world.L.tagpu_array_upload(self.h, _p(packed, _f64p), packed.size))
@@ -448,6 +488,10 @@ class DistArray:
             self.h, int(seed), int(stream), int(kind), None if ts is None else _p(ts, _f64p),
             int(compute_shape), np.float32(threshold)))
 
+    def truncate(self, threshold=-1.0):
+        """TiledArray::truncate: shape from the stored tiles' norms, small tiles dropped."""
+        self.world.check(self.world.L.tagpu_array_truncate(self.h, np.float32(threshold)))
+
     def tiles(self, trange: TiledRange):
         data = self.download()
         offs = self.tile_offsets()
@@ -474,6 +518,8 @@ class DistArray:
         return TsrExpr(self, indices)
 
     def __setitem__(self, indices: str, expr):
+        if isinstance(expr, _Accumulated) and expr.target.array is self:
+            return
         if not isinstance(expr, MultExpr):
             raise TypeError("only contractions A(...) * B(...) are on this path")
         opts = ContractOpts(self.precision, self.slices, -1.0, 0)
@@ -506,6 +552,16 @@ def contract(world, c_idx, alpha, A, a_idx, B, b_idx, precision=PRECISION_FP64, 
                                        a_idx.encode(), B.h, b_idx.encode(), ctypes.byref(opts),
                                        ctypes.byref(h)))
     return DistArray(world, _handle=h), world.last_stats()
+
+
+def contract_accumulate(world, C, c_idx, alpha, A, a_idx, B, b_idx, precision=PRECISION_FP64,
+                        slices=0, threshold=-1.0):
+    """C(c_idx) += alpha * A(a_idx) * B(b_idx) in place; returns the product's stats."""
+    opts = ContractOpts(precision, slices, threshold, 0)
+    world.check(world.L.tagpu_contract_accumulate(world.h, c_idx.encode(), float(alpha), A.h,
+                                                  a_idx.encode(), B.h, b_idx.encode(),
+                                                  ctypes.byref(opts), C.h))
+    return world.last_stats()
 
 
 class Server:

@@ -51,6 +51,14 @@ struct PermuteDesc {
   int rank;
   int perm[8];
 };
+// Tile-wise sum R = C + P over one run of elements of a result tile
+// (c or p < 0: that argument tile is absent and the other is copied).
+struct AddChunk {
+  int64_t r, c, p, len;
+};
+void launch_add_tiles(cudaStream_t s, const AddChunk* chunks, int64_t nchunks, const double* C,
+                      const double* P, double* R);
+
 void launch_permute(cudaStream_t s, const PermuteDesc& d, int64_t ntiles,
                     const int32_t* ext, const int64_t* in_off,
                     const int64_t* out_off, const int64_t* item_start,
@@ -125,7 +133,7 @@ void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int
 // Number of row chunks (1 unless the A digit bricks would not fit at once;
 // chunked plans are launched on their own, not grouped with others).
 int ozaki_chunks(const OzakiPlan* pl);
-// Times the block-order and chunk schedules on this contraction and applies
+// Times the block-order schedules on this contraction and applies
 // the fastest; cache: file of tuned buckets (NULL or "" = no cache).
 tagpu_status ozaki_autotune(OzakiPlan* pl, int sm_count, cudaStream_t s, const char* cache,
                             std::string* log, std::string* err);

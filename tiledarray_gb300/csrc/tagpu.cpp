@@ -666,6 +666,60 @@ tagpu_status tagpu_array_download(const tagpu_array* a, double* tiles, int64_t n
   return TAGPU_OK;
 }
 
+// After a shape change: the stored tiles `present` (ordinal order, at element
+// offsets `offs` of a->data) move to the offsets of the tiles the new shape
+// keeps.  Compaction is in place: surviving tiles move to lower addresses in
+// ordinal order; a tile whose source and destination overlap goes through a
+// bounce buffer of one tile, disjoint runs are single copies.
+static tagpu_status compact_tiles(tagpu_ctx* ctx, tagpu_array* a,
+                                  const std::vector<int64_t>& present,
+                                  const std::vector<int64_t>& offs) {
+  tagpu_status st;
+  const int64_t np = (int64_t)present.size();
+  pack_offsets(a);  // offsets of the tiles that survived the shape
+  DBuf bounce(ctx);
+  int64_t x = 0;
+  while (x < np) {
+    const int64_t t = present[x];
+    const int64_t dst = a->off[t];
+    if (dst < 0 || dst == offs[x]) {
+      ++x;
+      continue;
+    }
+    const int64_t len = offs[x + 1] - offs[x];
+    if (dst + len <= offs[x]) {
+      CUDA_TRY(ctx, cudaMemcpyAsync(a->data + dst, a->data + offs[x], len * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, ctx->stream));
+    } else {
+      if (bounce.n < (size_t)len * sizeof(double) && (st = bounce.alloc(len * sizeof(double))))
+        return st;
+      CUDA_TRY(ctx, cudaMemcpyAsync(bounce.p, a->data + offs[x], len * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, ctx->stream));
+      CUDA_TRY(ctx, cudaMemcpyAsync(a->data + dst, bounce.p, len * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    ++x;
+  }
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  // release the tail the dropped tiles occupied (kept if no room to move)
+  const size_t keep = (size_t)a->elements * sizeof(double);
+  if (keep < a->bytes) {
+    void* p = nullptr;
+    if (keep && (st = dev_alloc(ctx, &p, keep)) == TAGPU_OK) {
+      CUDA_TRY(ctx, cudaMemcpyAsync(p, a->data, keep, cudaMemcpyDeviceToDevice, ctx->stream));
+      dev_free(ctx, a->data, a->bytes);
+      a->data = static_cast<double*>(p);
+      a->bytes = keep;
+    } else if (!keep) {
+      dev_free(ctx, a->data, a->bytes);
+      a->data = nullptr;
+      a->bytes = 0;
+    }
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  return TAGPU_OK;
+}
+
 tagpu_status tagpu_array_generate(tagpu_array* a, uint64_t seed, uint64_t stream, int kind,
                                   const double* tile_scale, int compute_shape,
                                   float threshold) {
@@ -741,51 +795,42 @@ tagpu_status tagpu_array_generate(tagpu_array* a, uint64_t seed, uint64_t stream
     a->norms = norms;
     a->zero_count = scale_norms(a, a->norms, thr);
   }
-  pack_offsets(a);  // offsets of the tiles that survived the shape
-  // Compact in place: surviving tiles move to lower addresses in ordinal
-  // order.  A tile whose source and destination overlap goes through a
-  // bounce buffer of one tile; disjoint runs are single copies.
-  DBuf bounce(ctx);
-  int64_t x = 0;
-  while (x < np) {
-    const int64_t t = present[x];
-    const int64_t dst = a->off[t];
-    if (dst < 0 || dst == offs[x]) {
-      ++x;
-      continue;
-    }
-    const int64_t len = offs[x + 1] - offs[x];
-    if (dst + len <= offs[x]) {
-      CUDA_TRY(ctx, cudaMemcpyAsync(a->data + dst, a->data + offs[x], len * sizeof(double),
-                                    cudaMemcpyDeviceToDevice, ctx->stream));
-    } else {
-      if (bounce.n < (size_t)len * sizeof(double) && (st = bounce.alloc(len * sizeof(double))))
-        return st;
-      CUDA_TRY(ctx, cudaMemcpyAsync(bounce.p, a->data + offs[x], len * sizeof(double),
-                                    cudaMemcpyDeviceToDevice, ctx->stream));
-      CUDA_TRY(ctx, cudaMemcpyAsync(a->data + dst, bounce.p, len * sizeof(double),
-                                    cudaMemcpyDeviceToDevice, ctx->stream));
-    }
-    ++x;
+  return compact_tiles(ctx, a, present, offs);
+}
+
+tagpu_status tagpu_array_truncate(tagpu_array* a, float threshold) {
+  if (!a) return TAGPU_ERR_INVALID;
+  tagpu_ctx* ctx = a->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  if (a->dense) return TAGPU_OK;   // DensePolicy: no-op
+  cudaSetDevice(ctx->device);
+  const float thr = threshold < 0 ? ctx->threshold : threshold;
+  const int64_t n = a->ntiles();
+  std::vector<int64_t> present, offs(1, 0);
+  for (int64_t t = 0; t < n; ++t) {
+    if (a->off[t] < 0) continue;
+    present.push_back(t);
+    offs.push_back(offs.back() + a->tile_volume(t));
   }
+  const int64_t np = (int64_t)present.size();
+  tagpu_status st;
+  DBuf doff(ctx), dn(ctx);
+  if ((st = upload_vec(ctx, doff, offs)) ||
+      (st = dn.alloc(std::max<int64_t>(1, np) * sizeof(float))))
+    return st;
+  launch_tile_norms(ctx->stream, np, doff.as<int64_t>(), a->data, dn.as<float>());
+  CUDA_TRY(ctx, cudaGetLastError());
+  std::vector<float> pn(np);
+  if (np)
+    CUDA_TRY(ctx, cudaMemcpyAsync(pn.data(), dn.p, np * sizeof(float), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  // release the tail the dropped tiles occupied
-  const size_t keep = (size_t)a->elements * sizeof(double);
-  if (keep < a->bytes) {
-    void* p = nullptr;
-    if (keep && (st = dev_alloc(ctx, &p, keep)) == TAGPU_OK) {
-      CUDA_TRY(ctx, cudaMemcpyAsync(p, a->data, keep, cudaMemcpyDeviceToDevice, ctx->stream));
-      dev_free(ctx, a->data, a->bytes);
-      a->data = static_cast<double*>(p);
-      a->bytes = keep;
-    } else if (!keep) {
-      dev_free(ctx, a->data, a->bytes);
-      a->data = nullptr;
-      a->bytes = 0;
-    }
-    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  }
-  return TAGPU_OK;
+  std::vector<float> norms(n, 0.0f);
+  for (int64_t x = 0; x < np; ++x) norms[present[x]] = pn[x];
+  a->threshold = thr;
+  a->norms = norms;
+  a->zero_count = scale_norms(a, a->norms, thr);
+  return compact_tiles(ctx, a, present, offs);
 }
 
 tagpu_status tagpu_array_get_info(const tagpu_array* a, tagpu_array_info* info) {
@@ -818,6 +863,29 @@ tagpu_status tagpu_array_get_norms(const tagpu_array* a, float* norms) {
 tagpu_status tagpu_array_get_tile_offsets(const tagpu_array* a, int64_t* offsets) {
   if (!a || !offsets) return TAGPU_ERR_INVALID;
   std::copy(a->off.begin(), a->off.end(), offsets);
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_array_get_tile(const tagpu_array* a, int64_t ordinal, double* tile,
+                                  int64_t n) {
+  if (!a) return TAGPU_ERR_INVALID;
+  tagpu_ctx* ctx = a->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  if (ordinal < 0 || ordinal >= (int64_t)a->off.size())
+    return fail(ctx, TAGPU_ERR_INVALID, "get_tile: ordinal %lld outside the tile grid",
+                (long long)ordinal);
+  if (a->off[ordinal] < 0)
+    return fail(ctx, TAGPU_ERR_INVALID, "get_tile: tile %lld is zero", (long long)ordinal);
+  const int64_t vol = a->tile_volume(ordinal);
+  if (n != vol)
+    return fail(ctx, TAGPU_ERR_INVALID, "get_tile: buffer holds %lld elements, tile %lld",
+                (long long)n, (long long)vol);
+  if (n && !tile) return fail(ctx, TAGPU_ERR_INVALID, "get_tile: null buffer");
+  cudaSetDevice(ctx->device);
+  if (n)
+    CUDA_TRY(ctx, cudaMemcpyAsync(tile, a->data + a->off[ordinal], n * sizeof(double),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return TAGPU_OK;
 }
 
@@ -1504,6 +1572,80 @@ tagpu_status tagpu_contract(tagpu_ctx* ctx, const char* c_idx, double alpha, tag
   cudaSetDevice(ctx->device);
   *c = nullptr;
   return contract_impl(ctx, c_idx, alpha, A, a_idx, B, b_idx, opts, c, &ctx->last);
+}
+
+tagpu_status tagpu_contract_accumulate(tagpu_ctx* ctx, const char* c_idx, double alpha,
+                                       tagpu_array* A, const char* a_idx, tagpu_array* B,
+                                       const char* b_idx, const tagpu_contract_opts* opts,
+                                       tagpu_array* C) {
+  if (!ctx || !A || !B || !C) return ctx ? fail(ctx, TAGPU_ERR_INVALID, "null argument")
+                                         : TAGPU_ERR_INVALID;
+  if (A->ctx != ctx || B->ctx != ctx || C->ctx != ctx)
+    return fail(ctx, TAGPU_ERR_INVALID, "arrays belong to another context");
+  if (C == A || C == B)
+    return fail(ctx, TAGPU_ERR_INVALID, "accumulate: the target may not be an argument");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  tagpu_array* p = nullptr;
+  tagpu_status st = contract_impl(ctx, c_idx, alpha, A, a_idx, B, b_idx, opts, &p, &ctx->last);
+  if (st) return st;
+  std::unique_ptr<tagpu_array> P(p);
+  if (P->rank != C->rank || P->hm != C->hm)
+    return fail(ctx, TAGPU_ERR_INVALID, "accumulate: the target's tiling differs from the product's");
+  if (P->dense != C->dense)
+    return fail(ctx, TAGPU_ERR_UNSUPPORTED, "accumulate: dense and sparse policies mixed");
+  // result shape: SparseShape::add (sparse_shape.h:1309-1328), float sum of the
+  // scaled norms, zeroed below the threshold in force
+  tagpu_array R;   // the result: C's tiling and policy, storage of its own
+  R.ctx = ctx;
+  R.rank = C->rank;
+  R.hm = C->hm;
+  R.nt = C->nt;
+  R.dense = C->dense;
+  if (!C->dense) {
+    const int64_t n = C->ntiles();
+    R.threshold = ctx->threshold;
+    R.norms.assign(n, 0.0f);
+    R.zero_count = 0;
+    for (int64_t t = 0; t < n; ++t) {
+      float v = C->norms[t] + P->norms[t];
+      if (v < R.threshold) {
+        v = 0.0f;
+        ++R.zero_count;
+      }
+      R.norms[t] = v;
+    }
+  }
+  pack_offsets(&R);
+  if ((st = ensure_storage(&R))) return st;
+  std::vector<AddChunk> chunks;
+  const int64_t kChunk = 1 << 14;
+  for (int64_t t = 0; t < (int64_t)R.off.size(); ++t) {
+    if (R.off[t] < 0) continue;
+    const int64_t c = C->off[t], q = P->off[t], vol = R.tile_volume(t);
+    if (c < 0 && q < 0) {
+      CUDA_TRY(ctx, cudaMemsetAsync(R.data + R.off[t], 0, vol * sizeof(double), ctx->stream));
+      continue;
+    }
+    for (int64_t x = 0; x < vol; x += kChunk)
+      chunks.push_back({R.off[t] + x, c < 0 ? -1 : c + x, q < 0 ? -1 : q + x,
+                        std::min(kChunk, vol - x)});
+  }
+  DBuf dch(ctx);
+  if ((st = upload_vec(ctx, dch, chunks))) return st;
+  launch_add_tiles(ctx->stream, dch.as<AddChunk>(), (int64_t)chunks.size(), C->data, P->data,
+                   R.data);
+  CUDA_TRY(ctx, cudaGetLastError());
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  // C takes the result; its old storage leaves with R
+  std::swap(C->norms, R.norms);
+  std::swap(C->threshold, R.threshold);
+  std::swap(C->zero_count, R.zero_count);
+  std::swap(C->off, R.off);
+  std::swap(C->elements, R.elements);
+  std::swap(C->data, R.data);
+  std::swap(C->bytes, R.bytes);
+  return TAGPU_OK;
 }
 
 tagpu_status tagpu_batch_create(tagpu_ctx* ctx, tagpu_batch** out) {
