@@ -52,6 +52,20 @@ def workload(n=16384, seed=0, lo=48, hi=256, decay=4.0, cut=1e-10):
     return h, scale
 
 
+def profiled_traffic(name):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary profiles/<name> (line `traffic_bytes_per_launch: N`), or None."""
+    p = os.path.join(ROOT, "profiles", name)
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -575,6 +589,15 @@ def main():
                 "frac": achieved / bf16_peak, "traffic": None,
                 "kernel": "ozaki_gemm (bf16 digit-slice products, "
                           f"{pairs_per} per FP64 product)", "peak_kind": f"{peak_kind} bf16 burst"}
+        if args.n == 16384 and args.slices == 6 and args.seed == 0:
+            tb = profiled_traffic("ozaki_gemm_blocksparse.md")
+            if tb:
+                roof["traffic"] = tb
+                roof["traffic_note"] = (
+                    "DRAM bytes of this launch from one ncu capture of the same command "
+                    f"(profiles/ozaki_gemm_blocksparse.md): {tb / (gemm_ms * 1e-3) / 1e9:.0f} "
+                    f"GB/s over the timed GEMM = {tb / (gemm_ms * 1e-3) / 1e9 / hbm_peak:.2f} "
+                    "of measured HBM")
     else:
         achieved = flops / (gemm_ms * 1e-3) / 1e12
         dmma_peak, _ = w.fp64_rates()
@@ -622,22 +645,29 @@ def main():
         a_host[:] = A.download()
         b_host[:] = B.download()
         c_host = None
-        e2e_ms = []
+        C2, _ = step()   # the result's pinned host buffer is allocated outside the timing
+        c_host = torch.empty(C2.info().elements, dtype=torch.float64, pin_memory=True).numpy()
+        del C2
+        e2e_ms, parts = [], []
         for _ in range(max(1, min(args.steps, 3))):
             t0 = time.perf_counter()
             A.upload(a_host)
             B.upload(b_host)
+            t1 = time.perf_counter()
             C2, st2 = step()
+            t2 = time.perf_counter()
             n = C2.info().elements
-            if c_host is None:
-                c_host = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
             w.check(w.L.tagpu_array_download(C2.h, c_host.ctypes.data_as(ta._f64p), n))
-            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+            t3 = time.perf_counter()
+            e2e_ms.append((t3 - t0) * 1e3)
+            parts.append(((t1 - t0) * 1e3, (t2 - t1) * 1e3, (t3 - t2) * 1e3))
             del C2
         e = statistics.median(e2e_ms)
+        pm = parts[e2e_ms.index(e)] if e in e2e_ms else parts[0]
         out["e2e"] = {"value": flops / (e * 1e-3) / 1e12, "unit": "TFLOP/s",
                       "h2d_bytes_per_step": int(a_host.nbytes + b_host.nbytes),
-                      "d2h_bytes_per_step": int(c_host.nbytes), "ms_per_step": e}
+                      "d2h_bytes_per_step": int(c_host.nbytes), "ms_per_step": e,
+                      "phases_ms": {"h2d": pm[0], "contract": pm[1], "d2h": pm[2]}}
         if not args.no_cpu:
             A_t = {"data": a_host, "offsets": A.tile_offsets(), "norms": A.norms()}
             B_t = {"data": b_host, "offsets": B.tile_offsets(), "norms": B.norms()}
