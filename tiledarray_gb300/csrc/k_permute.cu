@@ -11,6 +11,10 @@
 //     staged through shared memory so that both the load (along a) and the
 //     store (along b) are coalesced; all other dimensions form the batch.
 // All tiles of one array share the permutation; extents differ per tile.
+// Index arithmetic is paid per item, not per element: a row-copy item is
+// kRowsPerItem rows whose offsets are computed once into shared memory and
+// then copied as one flat, coalesced element range; a transpose item is a
+// strip of 32 x 32 blocks along the result's fastest dimension.
 #include <cuda_runtime.h>
 
 #include "internal.h"
@@ -18,7 +22,7 @@
 namespace tagpu {
 namespace {
 
-constexpr int kRowsPerItem = 8;
+constexpr int kRowsPerItem = 128;
 
 struct TileGeom {
   int64_t e[8];       // argument extents
@@ -63,7 +67,7 @@ __host__ __device__ inline int64_t items_of(const TileGeom& g) {
     return (rows + kRowsPerItem - 1) / kRowsPerItem;
   }
   const int64_t batch = g.vol / (g.e[g.a] * g.e[g.b]);
-  return batch * ((g.e[g.a] + 31) / 32) * ((g.e[g.b] + 31) / 32);
+  return batch * ((g.e[g.a] + 31) / 32);
 }
 
 // offsets of the batch index `bi` over all dims except `skip0`/`skip1`
@@ -86,6 +90,7 @@ __global__ void __launch_bounds__(256) permute_kernel(
     const int64_t* __restrict__ item_start, int64_t nitems,
     const double* __restrict__ in, double* __restrict__ out) {
   __shared__ double buf[32][33];
+  __shared__ int64_t s_io[kRowsPerItem], s_oo[kRowsPerItem];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
   for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
     // tile owning this item
@@ -104,35 +109,56 @@ __global__ void __launch_bounds__(256) permute_kernel(
       const int64_t rowlen = g.e[g.a];
       const int64_t rows = g.vol / rowlen;
       const int64_t r0 = local * kRowsPerItem;
-      for (int rr = ty; rr < kRowsPerItem; rr += 8) {
-        const int64_t row = r0 + rr;
-        if (row >= rows) break;
+      const int nr = (int)(rows - r0 < kRowsPerItem ? rows - r0 : kRowsPerItem);
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) {
         int64_t io, oo;
-        batch_offsets(g, d.rank, g.a, -1, row, io, oo);
-        for (int64_t c = tx; c < rowlen; c += 32) dst[oo + c] = src[io + c];
+        batch_offsets(g, d.rank, g.a, -1, r0 + i, io, oo);
+        s_io[i] = io;
+        s_oo[i] = oo;
       }
+      __syncthreads();
+      // one warp per row; 16-byte accesses when both ends are aligned
+      for (int row = ty; row < nr; row += 8) {
+        const double* sp = src + s_io[row];
+        double* dp = dst + s_oo[row];
+        if (((((uintptr_t)sp) | ((uintptr_t)dp)) & 15) == 0) {
+          const int64_t half = rowlen >> 1;
+          const double2* s2 = reinterpret_cast<const double2*>(sp);
+          double2* d2 = reinterpret_cast<double2*>(dp);
+#pragma unroll 2
+          for (int64_t c = tx; c < half; c += 32) d2[c] = s2[c];
+          if ((rowlen & 1) && tx == 0) dp[rowlen - 1] = sp[rowlen - 1];
+        } else {
+#pragma unroll 2
+          for (int64_t c = tx; c < rowlen; c += 32) dp[c] = sp[c];
+        }
+      }
+      __syncthreads();
     } else {
+      // strip: batch index bi, block ab along a; all blocks along b
       const int64_t ea = g.e[g.a], eb = g.e[g.b];
-      const int64_t na = (ea + 31) / 32, nb = (eb + 31) / 32;
-      const int64_t per_batch = na * nb;
-      const int64_t bi = local / per_batch;
-      const int64_t rem = local - bi * per_batch;
-      const int64_t ab = rem % na, bb = rem / na;
+      const int64_t na = (ea + 31) / 32;
+      const int64_t bi = local / na, ab = local - bi * na;
       int64_t io, oo;
       batch_offsets(g, d.rank, g.a, g.b, bi, io, oo);
-      const int64_t a0 = ab * 32, b0 = bb * 32;
-      // load: along a (stride 1 in the argument)
-      for (int yy = ty; yy < 32; yy += 8) {
-        const int64_t ib = b0 + yy, ia = a0 + tx;
-        if (ib < eb && ia < ea) buf[yy][tx] = src[io + ib * g.is[g.b] + ia];
+      const int64_t a0 = ab * 32;
+      const int64_t isb = g.is[g.b], osa = g.os[g.a];
+      for (int64_t b0 = 0; b0 < eb; b0 += 32) {
+        // load: along a (stride 1 in the argument)
+#pragma unroll
+        for (int yy = ty; yy < 32; yy += 8) {
+          const int64_t ib = b0 + yy, ia = a0 + tx;
+          if (ib < eb && ia < ea) buf[yy][tx] = src[io + ib * isb + ia];
+        }
+        __syncthreads();
+        // store: along b (stride 1 in the result)
+#pragma unroll
+        for (int yy = ty; yy < 32; yy += 8) {
+          const int64_t ia = a0 + yy, ib = b0 + tx;
+          if (ib < eb && ia < ea) dst[oo + ia * osa + ib] = buf[tx][yy];
+        }
+        __syncthreads();
       }
-      __syncthreads();
-      // store: along b (stride 1 in the result)
-      for (int yy = ty; yy < 32; yy += 8) {
-        const int64_t ia = a0 + yy, ib = b0 + tx;
-        if (ib < eb && ia < ea) dst[oo + ia * g.os[g.a] + ib] = buf[tx][yy];
-      }
-      __syncthreads();
     }
   }
 }
