@@ -143,7 +143,22 @@ int ozaki_slices(const OzakiPlan* pl);
 int* ozaki_error_flag(OzakiPlan* pl);
 int ozaki_error(OzakiPlan* pl);   // synchronises; 0 = ok
 size_t ozaki_scratch_bytes(const OzakiPlan* pl);
-int64_t ozaki_blocks(const OzakiPlan* pl);
+// Frames and digit splits of several plans of one digit count (none split in
+// row chunks) in one launch per step: the host builds the job tables (bytes
+// to upload as they are), the enqueue runs zeroing, frames, B and A splits.
+struct OzGroupDims {
+  int nzero = 0, nframe = 0, nsplit_a = 0, nsplit_b = 0;
+  int64_t frame_tiles = 0, frame_rows = 0, split_a_bricks = 0, split_b_bricks = 0;
+};
+void ozaki_group_tables(OzakiPlan* const* pls, int n, std::vector<uint8_t>* zero_jobs,
+                        std::vector<uint8_t>* frame_jobs, std::vector<uint8_t>* split_a,
+                        std::vector<uint8_t>* split_b, OzGroupDims* d);
+void ozaki_group_enqueue(const void* zero_jobs, const void* frame_jobs, const void* split_a,
+                         const void* split_b, const OzGroupDims& d, int S, int sm_count,
+                         cudaStream_t s);
+// Units of the GEMM schedule (a unit is a pair of output blocks run by the
+// two CTAs of a cluster); multi-view launches offset their views by these.
+int64_t ozaki_units(const OzakiPlan* pl);
 void ozaki_destroy(OzakiPlan* pl);
 
 }  // namespace tagpu

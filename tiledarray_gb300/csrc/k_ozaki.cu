@@ -139,11 +139,38 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
       ::"r"(dst), "l"(src), "r"(bytes), "r"(mbar)
       : "memory");
 }
+// The same copy into the same shared-memory offset of every CTA of the
+// cluster in `mask`; each destination's mbarrier (same offset) gets the bytes.
+__device__ __forceinline__ void bulk_g2s_mc(uint32_t dst, const void* src, uint32_t bytes,
+                                            uint32_t mbar, uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+      " [%0], [%1], %2, [%3], %4;"
+      ::"r"(dst), "l"(src), "r"(bytes), "r"(mbar), "h"(mask)
+      : "memory");
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n"
+               "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
 __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// Arrive on the mbarrier at this offset in every CTA of `mask` once the
+// MMAs issued so far have completed.
+__device__ __forceinline__ void tc_commit_mc(uint32_t mbar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
+      " [%0], %1;" ::"r"(mbar), "h"(mask)
+      : "memory");
 }
 __device__ __forceinline__ void tc_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
@@ -258,7 +285,8 @@ struct OzParams {
   const int32_t* brickB;     // KBn x CB -> slot or -1
   const int32_t* blk;        // nblk x 2 (rb, cb), in scheduling order
   const int64_t* blk_rng;    // nblk x 2: [begin, end) of the block's k blocks in blk_kb
-  const int2* blk_ab;        // per k block of a block: (A brick slot, B brick slot)
+  const int4* blk_ab;        // per k block of a unit: A slot, B slots of its two column
+                             // blocks (the zero brick where absent), unused
   int64_t nblk;
   int KBn, CB;
   const int32_t* EA;         // M_total frames (biased exponent; E = EA - 1022)
@@ -296,7 +324,7 @@ __device__ __forceinline__ int find_view(const int64_t* __restrict__ vstart, int
 }
 
 template <int S>
-__global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
     const OzParams* __restrict__ views, const int64_t* __restrict__ vstart, int nviews,
     int64_t nblk_total, int* __restrict__ err) {
   constexpr int STAGES = Smem<S>::kStages;
@@ -310,11 +338,15 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint8_t* stage_base = (uint8_t*)(((uintptr_t)smem + 1023) & ~(uintptr_t)1023);
+  // The two CTAs of a cluster run the two output blocks of a unit: rank r
+  // owns column block 2c + r; each loads half of the shared A brick into both.
+  const uint32_t rank = cluster_rank();
+  const int64_t unit0 = blockIdx.x >> 1, unit_step = gridDim.x >> 1;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(smem_u32(&bar_full[s]), 1);
-      mbar_init(smem_u32(&bar_empty[s]), 1);
+      mbar_init(smem_u32(&bar_empty[s]), 2);   // both CTAs' MMAs have read the stage
     }
     mbar_init(smem_u32(&bar_acc_full), 1);
     for (int t = 0; t <= TOP; ++t) mbar_init(smem_u32(&bar_level[t]), EPI_WARPS * 32);
@@ -329,6 +361,7 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
   }
   tc_fence_before();
   __syncthreads();
+  cluster_sync();   // the partner's barriers exist before any multicast or remote arrive
   tc_fence_after();
   const uint32_t tmem = tmem_base_s;
   // level t (2..TOP) accumulates in tensor-memory columns [(t-2)*BN, (t-1)*BN)
@@ -348,18 +381,18 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
     bool issued[STAGES];
     for (int s = 0; s < STAGES; ++s) issued[s] = false;
     bool ok = true;
-    for (int64_t gb = blockIdx.x; gb < nblk_total && ok; gb += gridDim.x) {
+    for (int64_t gb = unit0; gb < nblk_total && ok; gb += unit_step) {
       const int vi = find_view(vstart, nviews, gb);
       const OzParams& P = views[vi];
       const int64_t b = gb - vstart[vi];
       const int64_t x0 = P.blk_rng[2 * b], x1 = P.blk_rng[2 * b + 1];
       for (int64_t xb = x0; xb < x1 && ok; xb += 32) {
-        int2 mine = make_int2(0, 0);
+        int4 mine = make_int4(0, 0, 0, 0);
         if (xb + lane < x1) mine = P.blk_ab[xb + lane];
         const int cnt = (int)(x1 - xb < 32 ? x1 - xb : 32);
         for (int j = 0; j < cnt; ++j) {
           const int sa = __shfl_sync(0xffffffffu, mine.x, j);
-          const int sb = __shfl_sync(0xffffffffu, mine.y, j);
+          const int sb = __shfl_sync(0xffffffffu, rank ? mine.z : mine.y, j);
           if (lane == 0) {
             if (!mbar_wait(smem_u32(&bar_empty[stage]), phase ^ 1, &abort_s)) {
               fail(1);
@@ -367,10 +400,14 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
             } else {
               uint8_t* dst = stage_base + stage * STAGE_BYTES;
               const uint32_t full = smem_u32(&bar_full[stage]);
+              // this CTA's half of the shared A brick into both CTAs, then its
+              // own B brick; the full stage (both A halves + B) completes here
+              constexpr uint32_t kHalfA = S * A_SLICE_BYTES / 2;   // multiple of 16
               mbar_expect_tx(full, STAGE_BYTES);
-              bulk_g2s(smem_u32(dst),
-                       P.Apack + (size_t)(sa - P.a_slot_base) * (S * A_SLICE_BYTES),
-                       S * A_SLICE_BYTES, full);
+              bulk_g2s_mc(smem_u32(dst) + rank * kHalfA,
+                          P.Apack + (size_t)(sa - P.a_slot_base) * (S * A_SLICE_BYTES) +
+                              rank * kHalfA,
+                          kHalfA, full, (uint16_t)3);
               bulk_g2s(smem_u32(dst + S * A_SLICE_BYTES),
                        P.Bpack + (size_t)sb * (S * B_SLICE_BYTES), S * B_SLICE_BYTES, full);
               issued[stage] = true;
@@ -447,7 +484,7 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
       level_used |= 1u << t;
       return true;
     };
-    for (int64_t gb = blockIdx.x; gb < nblk_total && ok; gb += gridDim.x) {
+    for (int64_t gb = unit0; gb < nblk_total && ok; gb += unit_step) {
       const int vi = find_view(vstart, nviews, gb);
       const OzParams& P = views[vi];
       const int64_t b = gb - vstart[vi];
@@ -526,7 +563,8 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
           }
         }
         __syncwarp();
-        if (lane == 0) tc_commit(smem_u32(&bar_empty[stage]));
+        // both CTAs write into this stage (the A halves): release it in both
+        if (lane == 0) tc_commit_mc(smem_u32(&bar_empty[stage]), (uint16_t)3);
         __syncwarp();
         if (++stage == STAGES) {
           stage = 0;
@@ -564,11 +602,11 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
     int64_t hi[32], lo[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j) hi[j] = lo[j] = 0;
-    for (int64_t gb = blockIdx.x; gb < nblk_total && ok; gb += gridDim.x) {
+    for (int64_t gb = unit0; gb < nblk_total && ok; gb += unit_step) {
       const int vi = find_view(vstart, nviews, gb);
       const OzParams& P = views[vi];
       const int64_t b = gb - vstart[vi];
-      const int rb = P.blk[2 * b], cb = P.blk[2 * b + 1];
+      const int rb = P.blk[2 * b], cb = 2 * P.blk[2 * b + 1] + (int)rank;
       const int64_t n = P.blk_rng[2 * b + 1] - P.blk_rng[2 * b];
       for (int64_t x = 0; x < n; ++x) {
         const uint32_t dm = drain_mask<TOP>(x, n);
@@ -642,6 +680,9 @@ __global__ void __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
   }
   tc_fence_before();
   __syncthreads();
+  // the partner no longer copies into this CTA's shared memory nor arrives on
+  // its barriers once it has passed this point
+  cluster_sync();
   tc_fence_after();
   if (warp == 1) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
@@ -669,113 +710,209 @@ __device__ __forceinline__ int exp_field(double x) {
   return (int)((__double_as_longlong(x) >> 52) & 0x7ff);
 }
 
-// One CTA per operand tile: max biased exponent of each of its rows over the
-// tile's k, folded into the row's frame with atomicMax.  Both storage orders
-// are read coalesced: rows of a row-major tile by warps along k, columns of a
+// A frame job: one operand of one contraction.  Tiles of all jobs of a
+// launch are numbered consecutively from each job's tile0.
+struct FrameJob {
+  OperandView v;
+  const int32_t* row_start;   // first fused row of every row tile
+  int32_t* E;                 // frames of the operand's fused rows
+  int64_t tile0;
+};
+
+// Frames: max biased exponent of every operand row over its k, folded into
+// the row's frame with atomicMax.  Grid x = operand tile (rt, kt) over all
+// jobs, grid y = chunk of kFrameRows rows of that tile, so long fused rows
+// and tall tiles both spread over many CTAs.  Both storage orders are read
+// coalesced: rows of a row-major tile by warps along k, columns of a
 // transposed tile by threads along the rows.
-__global__ void __launch_bounds__(256) frame_kernel(OperandView v,
-                                                    const int32_t* __restrict__ row_start,
-                                                    int32_t* __restrict__ E) {
-  const int64_t t = blockIdx.x;   // tile (rt, kt), rt-major
+constexpr int kFrameRows = 64;
+__global__ void __launch_bounds__(256) frame_kernel(const FrameJob* __restrict__ jobs,
+                                                    int njobs) {
+  int lo = 0, hi = njobs;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (jobs[mid].tile0 <= (int64_t)blockIdx.x) lo = mid; else hi = mid;
+  }
+  const FrameJob& J = jobs[lo];
+  const OperandView& v = J.v;
+  const int64_t t = (int64_t)blockIdx.x - J.tile0;   // tile (rt, kt), rt-major
+  if (t >= v.rowt * v.kt) return;
   const int64_t rt = t / v.kt, ktile = t - (t / v.kt) * v.kt;
   const int64_t o = v.off[rt * v.off_stride_row + ktile * v.off_stride_k];
   if (o < 0) return;
   const int m = v.rsz[rt], kk = v.ksz[ktile];
   const double* base = v.data + o;
-  int32_t* Er = E + row_start[rt];
-  if (v.row_contig) {              // element (r, k) at k * m + r
-    for (int r = threadIdx.x; r < m; r += blockDim.x) {
+  int32_t* Er = J.E + J.row_start[rt];
+  for (int r0 = blockIdx.y * kFrameRows; r0 < m; r0 += gridDim.y * kFrameRows) {
+    const int r1 = min(m, r0 + kFrameRows);
+    if (v.row_contig) {            // element (r, k) at k * m + r
+      const int r = r0 + (threadIdx.x % kFrameRows);
+      const int kq = threadIdx.x / kFrameRows, nq = blockDim.x / kFrameRows;
       int e = 0;
-      for (int k = 0; k < kk; ++k) e = max(e, exp_field(base[(int64_t)k * m + r]));
+      if (r < r1)
+        for (int k = kq; k < kk; k += nq) e = max(e, exp_field(base[(int64_t)k * m + r]));
       if (e > 0) atomicMax(&Er[r], e);
-    }
-  } else {                         // element (r, k) at r * kk + k
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int r = warp; r < m; r += blockDim.x >> 5) {
-      int e = 0;
-      for (int k = lane; k < kk; k += 32) e = max(e, exp_field(base[(int64_t)r * kk + k]));
-      for (int s = 16; s > 0; s >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, s));
-      if (lane == 0 && e > 0) atomicMax(&Er[r], e);
+    } else {                       // element (r, k) at r * kk + k
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      for (int r = r0 + warp; r < r1; r += blockDim.x >> 5) {
+        int e = 0;
+        for (int k = lane; k < kk; k += 32) e = max(e, exp_field(base[(int64_t)r * kk + k]));
+        for (int s = 16; s > 0; s >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, s));
+        if (lane == 0 && e > 0) atomicMax(&Er[r], e);
+      }
     }
   }
 }
 
-// One CTA per brick: gather ROWS x 32 elements, split into S digit slices,
-// write the brick image.
+// Zeroing of int32 ranges (frames, error flags) of many plans in one launch.
+struct ZeroJob {
+  int32_t* p;
+  int64_t n;
+};
+__global__ void zero_kernel(const ZeroJob* __restrict__ jobs) {
+  const ZeroJob J = jobs[blockIdx.x];
+  for (int64_t i = threadIdx.x; i < J.n; i += blockDim.x) J.p[i] = 0;
+}
+
+// Digits of one element into the brick image in shared memory:
+// fixed point round(x * 2^(8S-1-E)) (E = frame - 1022), cut into S balanced
+// base-256 digits, least significant first, each stored as exact bf16.
+template <int S, int SLICE>
+__device__ __forceinline__ void split_store(double x, int frame, int r, int k, uint8_t* img) {
+  int64_t fx = 0;
+  const uint64_t bits = (uint64_t)__double_as_longlong(x);
+  const int be = (int)((bits >> 52) & 0x7ff);
+  if (frame > 0 && (bits << 1) != 0) {
+    uint64_t mant = bits & 0xFFFFFFFFFFFFFull;
+    int bexp = be;
+    if (be == 0) {
+      bexp = 1;  // subnormal
+    } else {
+      mant |= 1ull << 52;
+    }
+    const int E = frame - 1022;
+    const int sh = 1075 + E - (8 * S - 1) - bexp;   // >= 53 - (8S - 1) >= 0 for S <= 6
+    uint64_t q;
+    if (sh <= 0) {
+      q = mant << (-sh);
+    } else if (sh >= 64) {
+      q = 0;
+    } else {
+      q = (mant >> sh) + ((mant >> (sh - 1)) & 1ull);  // round half up in magnitude
+    }
+    fx = (bits >> 63) ? -(int64_t)q : (int64_t)q;
+  }
+  int dig[S];
+#pragma unroll
+  for (int p = S - 1; p >= 1; --p) {
+    const int d = (int)(((fx + 128) & 255) - 128);
+    dig[p] = d;
+    fx = (fx - d) >> 8;
+  }
+  dig[0] = (int)fx;
+  const uint32_t bo = brick_offset(r, k);
+#pragma unroll
+  for (int p = 0; p < S; ++p)
+    *reinterpret_cast<uint16_t*>(img + p * SLICE + bo) =
+        (uint16_t)(__float_as_uint((float)dig[p]) >> 16);  // exact: |d| <= 128
+}
+
+// A split job: the bricks of one operand (or of one row chunk of it) of one
+// contraction.  Bricks of all jobs of a launch are numbered consecutively
+// from each job's brick0.
+struct SplitJob {
+  OperandView v;
+  const int32_t *row_tile, *row_local, *k_tile, *k_local;
+  const int32_t* E;           // frames of the operand's fused rows
+  int64_t rows_total, k_total;
+  const int32_t* bricks;      // nbricks x 2 (row block, k block)
+  int64_t nbricks;
+  uint8_t* pack;              // brick i of the job at pack + i * S * ROWS * 64 bytes
+  int64_t brick0;
+};
+
+// One CTA per brick (grid-stride over the bricks of all jobs): gather
+// ROWS x 32 elements, split them into S digit slices, write the brick image.
+// The brick's row and k maps (tile, local index, frame, tile extent) are
+// staged in shared memory first, so an element costs one tile-offset lookup
+// and one data load.  Row-major tiles are read by warps along rows with
+// lanes along k, transposed tiles with lanes along rows: both coalesced.
 template <int S, int ROWS>
-__global__ void __launch_bounds__(256) split_kernel(
-    OperandView v, const int32_t* __restrict__ row_tile, const int32_t* __restrict__ row_local,
-    const int32_t* __restrict__ k_tile, const int32_t* __restrict__ k_local,
-    const int32_t* __restrict__ E, int64_t rows_total, int64_t k_total,
-    const int32_t* __restrict__ bricks /* nbricks x 2 (rowblock, kblock) */, int64_t nbricks,
-    uint8_t* __restrict__ pack) {
+__global__ void __launch_bounds__(256) split_kernel(const SplitJob* __restrict__ jobs, int njobs,
+                                                    int64_t total) {
   constexpr int SLICE = ROWS * BK * 2;
   extern __shared__ __align__(16) uint8_t img[];
-  for (int64_t bi = blockIdx.x; bi < nbricks; bi += gridDim.x) {
-    const int rbk = bricks[2 * bi], kbk = bricks[2 * bi + 1];
-    for (int e = threadIdx.x; e < ROWS * BK; e += blockDim.x) {
-      int r, k;
-      if (v.row_contig) {
-        r = e % ROWS;
-        k = e / ROWS;
+  __shared__ int s_rt[ROWS], s_lr[ROWS], s_fr[ROWS], s_m[ROWS];
+  __shared__ int s_kt[BK], s_lk[BK], s_kk[BK];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  for (int64_t gbi = blockIdx.x; gbi < total; gbi += gridDim.x) {
+    int lo = 0, hi = njobs;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (jobs[mid].brick0 <= gbi) lo = mid; else hi = mid;
+    }
+    const SplitJob J = jobs[lo];
+    const OperandView& v = J.v;
+    const int32_t *row_tile = J.row_tile, *row_local = J.row_local;
+    const int32_t *k_tile = J.k_tile, *k_local = J.k_local, *E = J.E;
+    const int64_t rows_total = J.rows_total, k_total = J.k_total;
+    const int64_t bi = gbi - J.brick0;
+    const int rbk = J.bricks[2 * bi], kbk = J.bricks[2 * bi + 1];
+    for (int i = threadIdx.x; i < ROWS; i += blockDim.x) {
+      const int64_t gr = (int64_t)rbk * ROWS + i;
+      if (gr < rows_total) {
+        const int rt = row_tile[gr];
+        s_rt[i] = rt;
+        s_lr[i] = row_local[gr];
+        s_fr[i] = E[gr];
+        s_m[i] = v.rsz[rt];
       } else {
-        k = e % BK;
-        r = e / BK;
+        s_rt[i] = -1;
+        s_fr[i] = 0;
       }
-      const int64_t gr = (int64_t)rbk * ROWS + r, gk = (int64_t)kbk * BK + k;
-      double x = 0.0;
-      int frame = 0;
-      if (gr < rows_total && gk < k_total) {
-        const int rt = row_tile[gr], kt = k_tile[gk];
-        const int64_t o = v.off[(int64_t)rt * v.off_stride_row + (int64_t)kt * v.off_stride_k];
-        if (o >= 0) {
-          const int lr = row_local[gr], lk = k_local[gk];
-          const int m = v.rsz[rt], kk = v.ksz[kt];
-          x = v.row_contig ? v.data[o + (int64_t)lk * m + lr] : v.data[o + (int64_t)lr * kk + lk];
-        }
-        frame = E[gr];
+    }
+    if (threadIdx.x < BK) {
+      const int64_t gk = (int64_t)kbk * BK + threadIdx.x;
+      if (gk < k_total) {
+        const int kt = k_tile[gk];
+        s_kt[threadIdx.x] = kt;
+        s_lk[threadIdx.x] = k_local[gk];
+        s_kk[threadIdx.x] = v.ksz[kt];
+      } else {
+        s_kt[threadIdx.x] = -1;
       }
-      // fixed point: round(x * 2^(8S-1-E)), E = frame - 1022
-      int64_t fx = 0;
-      const uint64_t bits = (uint64_t)__double_as_longlong(x);
-      const int be = (int)((bits >> 52) & 0x7ff);
-      if (frame > 0 && (bits << 1) != 0) {
-        uint64_t mant = bits & 0xFFFFFFFFFFFFFull;
-        int bexp = be;
-        if (be == 0) {
-          bexp = 1;  // subnormal
-        } else {
-          mant |= 1ull << 52;
-        }
-        const int E = frame - 1022;
-        const int sh = 1075 + E - (8 * S - 1) - bexp;   // >= 53 - (8S - 1) >= 0 for S <= 6
-        uint64_t q;
-        if (sh <= 0) {
-          q = mant << (-sh);
-        } else if (sh >= 64) {
-          q = 0;
-        } else {
-          q = (mant >> sh) + ((mant >> (sh - 1)) & 1ull);  // round half up in magnitude
-        }
-        fx = (bits >> 63) ? -(int64_t)q : (int64_t)q;
-      }
-      // balanced base-256 digits, least significant first
-      int dig[S];
-#pragma unroll
-      for (int p = S - 1; p >= 1; --p) {
-        const int d = (int)(((fx + 128) & 255) - 128);
-        dig[p] = d;
-        fx = (fx - d) >> 8;
-      }
-      dig[0] = (int)fx;
-      const uint32_t bo = brick_offset(r, k);
-#pragma unroll
-      for (int p = 0; p < S; ++p)
-        *reinterpret_cast<uint16_t*>(img + p * SLICE + bo) =
-            (uint16_t)(__float_as_uint((float)dig[p]) >> 16);  // exact: |d| <= 128
     }
     __syncthreads();
-    uint4* dst = reinterpret_cast<uint4*>(pack + (size_t)bi * S * SLICE);
+    if (!v.row_contig) {
+      // element (r, k) at o + lr * kk + lk: lanes along k
+      const int k = lane, kt = s_kt[k], lk = s_lk[k], kk = kt >= 0 ? s_kk[k] : 0;
+#pragma unroll 4
+      for (int r = warp; r < ROWS; r += nwarps) {
+        const int rt = s_rt[r];
+        double x = 0.0;
+        if (rt >= 0 && kt >= 0) {
+          const int64_t o = v.off[(int64_t)rt * v.off_stride_row + (int64_t)kt * v.off_stride_k];
+          if (o >= 0) x = v.data[o + (int64_t)s_lr[r] * kk + lk];
+        }
+        split_store<S, SLICE>(x, s_fr[r], r, k, img);
+      }
+    } else {
+      // element (r, k) at o + lk * m + lr: lanes along rows
+#pragma unroll 4
+      for (int it = warp; it < BK * (ROWS / 32); it += nwarps) {
+        const int k = it % BK, r = (it / BK) * 32 + lane;
+        const int rt = s_rt[r], kt = s_kt[k];
+        double x = 0.0;
+        if (rt >= 0 && kt >= 0) {
+          const int64_t o = v.off[(int64_t)rt * v.off_stride_row + (int64_t)kt * v.off_stride_k];
+          if (o >= 0) x = v.data[o + (int64_t)s_lk[k] * s_m[r] + s_lr[r]];
+        }
+        split_store<S, SLICE>(x, s_fr[r], r, k, img);
+      }
+    }
+    __syncthreads();
+    uint4* dst = reinterpret_cast<uint4*>(J.pack + (size_t)bi * S * SLICE);
     const uint4* src = reinterpret_cast<const uint4*>(img);
     for (int i = threadIdx.x; i < S * SLICE / 16; i += blockDim.x) dst[i] = src[i];
     __syncthreads();
@@ -817,8 +954,26 @@ __global__ void brick_slot_kernel(const int64_t* __restrict__ flag,
   }
 }
 
-// One warp per output block: active if it overlaps a nonzero result tile;
-// count (emit) the k blocks whose A and B bricks both exist.
+// Units of work are pairs of output blocks (rb, 2c) and (rb, 2c+1), run by
+// the two CTAs of a cluster, which share the A brick of every k block.
+// One warp per unit: a column block is active if it overlaps a nonzero
+// result tile; the unit's k list is every k block whose A brick exists and
+// whose B brick exists for an active column block of the pair.
+__device__ __forceinline__ bool block_active(const int32_t* __restrict__ row_tile,
+                                             const int32_t* __restrict__ col_tile,
+                                             const int64_t* __restrict__ coff, int64_t Nt,
+                                             int64_t M_total, int64_t N_total, int64_t rb,
+                                             int64_t cb) {
+  const int64_t r0 = rb * BM, r1 = min(M_total, r0 + BM) - 1;
+  const int64_t c0 = cb * BN;
+  if (c0 >= N_total) return false;
+  const int64_t c1 = min(N_total, c0 + BN) - 1;
+  for (int it = row_tile[r0]; it <= row_tile[r1]; ++it)
+    for (int jt = col_tile[c0]; jt <= col_tile[c1]; ++jt)
+      if (coff[(int64_t)it * Nt + jt] >= 0) return true;
+  return false;
+}
+
 __global__ void block_kernel(const int32_t* __restrict__ brickA, const int32_t* __restrict__ brickB,
                              const int32_t* __restrict__ row_tile,
                              const int32_t* __restrict__ col_tile, const int64_t* __restrict__ coff,
@@ -826,24 +981,21 @@ __global__ void block_kernel(const int32_t* __restrict__ brickA, const int32_t* 
                              int64_t KB, const int64_t* __restrict__ offs /* null: count */,
                              int64_t* __restrict__ counts, int32_t* __restrict__ kbs) {
   const int lane = threadIdx.x & 31;
+  const int64_t CP = (CB + 1) / 2;
   const int64_t x = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (x >= RB * CB) return;
-  const int64_t rb = x / CB, cb = x - (x / CB) * CB;
-  const int64_t r0 = rb * BM, r1 = min(M_total, r0 + BM) - 1;
-  const int64_t c0 = cb * BN, c1 = min(N_total, c0 + BN) - 1;
-  bool active = false;
-  for (int it = row_tile[r0]; it <= row_tile[r1] && !active; ++it)
-    for (int jt = col_tile[c0]; jt <= col_tile[c1]; ++jt)
-      if (coff[(int64_t)it * Nt + jt] >= 0) {
-        active = true;
-        break;
-      }
+  if (x >= RB * CP) return;
+  const int64_t rb = x / CP, cp = x - (x / CP) * CP;
+  const int64_t cb0 = 2 * cp, cb1 = 2 * cp + 1;
+  const bool act0 = block_active(row_tile, col_tile, coff, Nt, M_total, N_total, rb, cb0);
+  const bool act1 =
+      cb1 < CB && block_active(row_tile, col_tile, coff, Nt, M_total, N_total, rb, cb1);
   int64_t cnt = 0;
   int64_t pos = offs ? offs[x] : 0;
-  if (active) {
+  if (act0 || act1) {
     for (int64_t k0 = 0; k0 < KB; k0 += 32) {
       const int64_t kb = k0 + lane;
-      const bool p = kb < KB && brickA[rb * KB + kb] >= 0 && brickB[kb * CB + cb] >= 0;
+      bool p = kb < KB && brickA[rb * KB + kb] >= 0;
+      if (p) p = (act0 && brickB[kb * CB + cb0] >= 0) || (act1 && brickB[kb * CB + cb1] >= 0);
       const unsigned bm = __ballot_sync(0xffffffffu, p);
       if (offs && p) kbs[pos + __popc(bm & ((1u << lane) - 1u))] = (int32_t)kb;
       pos += __popc(bm);
@@ -854,28 +1006,38 @@ __global__ void block_kernel(const int32_t* __restrict__ brickA, const int32_t* 
 }
 
 __global__ void block_list_kernel(const int64_t* __restrict__ counts,
-                                  const int64_t* __restrict__ scan_blocks, int64_t n, int64_t CB,
+                                  const int64_t* __restrict__ scan_blocks, int64_t n, int64_t CP,
                                   int32_t* __restrict__ blk) {
   const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= n || counts[x] == 0) return;
   const int64_t s = scan_blocks[x];
-  blk[2 * s] = (int32_t)(x / CB);
-  blk[2 * s + 1] = (int32_t)(x - (x / CB) * CB);
+  blk[2 * s] = (int32_t)(x / CP);
+  blk[2 * s + 1] = (int32_t)(x - (x / CP) * CP);
 }
 
-// Brick slots of every (output block, k block): one warp per output block.
+// Brick slots of every (unit, k block): one warp per unit.  A column block
+// without a B brick at this k (or past the last column, or inactive) reads
+// the zero brick `zero_b`.
 __global__ void slot_pairs_kernel(const int32_t* __restrict__ blk, const int64_t* __restrict__ off,
                                   int64_t nblk, const int32_t* __restrict__ kbs,
                                   const int32_t* __restrict__ brickA,
                                   const int32_t* __restrict__ brickB, int64_t KB, int64_t CB,
-                                  int2* __restrict__ out) {
+                                  const int32_t* __restrict__ row_tile,
+                                  const int32_t* __restrict__ col_tile,
+                                  const int64_t* __restrict__ coff, int64_t Nt, int64_t M_total,
+                                  int64_t N_total, int32_t zero_b, int4* __restrict__ out) {
   const int lane = threadIdx.x & 31;
   const int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (b >= nblk) return;
-  const int64_t rb = blk[2 * b], cb = blk[2 * b + 1];
+  const int64_t rb = blk[2 * b], cb0 = 2 * (int64_t)blk[2 * b + 1], cb1 = cb0 + 1;
+  const bool act0 = block_active(row_tile, col_tile, coff, Nt, M_total, N_total, rb, cb0);
+  const bool act1 =
+      cb1 < CB && block_active(row_tile, col_tile, coff, Nt, M_total, N_total, rb, cb1);
   for (int64_t x = off[b] + lane; x < off[b + 1]; x += 32) {
     const int64_t kb = kbs[x];
-    out[x] = make_int2(brickA[rb * KB + kb], brickB[kb * CB + cb]);
+    int32_t b0 = act0 ? brickB[kb * CB + cb0] : -1;
+    int32_t b1 = act1 ? brickB[kb * CB + cb1] : -1;
+    out[x] = make_int4(brickA[rb * KB + kb], b0 >= 0 ? b0 : zero_b, b1 >= 0 ? b1 : zero_b, 0);
   }
 }
 
@@ -919,10 +1081,18 @@ struct OzakiPlan {
   std::vector<DevVec> bufs;
   int32_t *row_tile = nullptr, *row_local = nullptr, *k_tile = nullptr, *k_local = nullptr,
           *col_tile = nullptr, *col_local = nullptr, *rstart = nullptr, *cstart = nullptr;
-  int2* blk_ab = nullptr;
+  int4* blk_ab = nullptr;
   int32_t *EA = nullptr, *EB = nullptr, *brickA = nullptr, *brickB = nullptr, *listA = nullptr,
           *listB = nullptr, *blk = nullptr, *blk_kb = nullptr;
   int64_t *blk_off = nullptr, *blk_rng = nullptr;
+  int64_t max_rows_a = 0, max_rows_b = 0;   // tallest row tile of each operand
+  // work tables of the frame and split launches (host copies and device)
+  FrameJob h_frames[2];                    // A, B
+  SplitJob h_split_b;
+  std::vector<SplitJob> h_split_a;         // one per row chunk
+  FrameJob* d_frames = nullptr;
+  SplitJob* d_split_b = nullptr;
+  SplitJob* d_split_a = nullptr;
   uint8_t *Apack = nullptr, *Bpack = nullptr;
   int* err = nullptr;
   OzParams P{};
@@ -937,7 +1107,7 @@ struct OzakiPlan {
   int64_t* d_chunk_vstart = nullptr;
   std::vector<int64_t> chunk_rb{0, 0};     // row-block boundaries of the chunks
   // schedule (results do not depend on it): super-tile of the block order
-  int tune_gr = 8, tune_gc = 19;
+  int tune_gr = 4, tune_gc = 19;
   std::vector<int32_t> h_blk;              // blocks (rb, cb) in discovery order
   std::vector<int64_t> h_off;              // their k-list offsets
   size_t bytes = 0;
@@ -986,7 +1156,8 @@ void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int
                          (int)smem);
     set[dev] = true;
   }
-  const int64_t grid = std::min<int64_t>(nblk, sm_count);
+  // clusters of two CTAs, one unit (pair of output blocks) at a time each
+  const int64_t grid = 2 * std::min<int64_t>(nblk, sm_count / 2);
   if (grid > 0) {
     ozaki_gemm_kernel<S><<<(unsigned)grid, THREADS, smem, st>>>(views, vstart, nviews, nblk, err);
     count_launch();
@@ -994,8 +1165,8 @@ void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int
 }
 
 template <int S>
-void launch_split_t(const OzakiPlan& pl, int sm_count, cudaStream_t st, bool do_a, int64_t a0,
-                    int64_t a1, bool do_b) {
+void launch_split_t(const SplitJob* d_jobs, int njobs, int64_t total, bool a_side,
+                    int sm_count, cudaStream_t st) {
   // the shared-memory attribute is per device
   static bool set[kMaxDevices] = {};
   int dev = 0;
@@ -1007,32 +1178,35 @@ void launch_split_t(const OzakiPlan& pl, int sm_count, cudaStream_t st, bool do_
                          S * B_SLICE_BYTES);
     set[dev] = true;
   }
-  const int64_t na = a1 - a0;
-  const int grid_a = (int)std::min<int64_t>(na, (int64_t)sm_count * 8);
-  const int grid_b = (int)std::min<int64_t>(pl.nB, (int64_t)sm_count * 8);
-  if (do_a && grid_a > 0) {
-    split_kernel<S, BM><<<grid_a, 256, S * A_SLICE_BYTES, st>>>(
-        pl.va, pl.row_tile, pl.row_local, pl.k_tile, pl.k_local, pl.EA, pl.M_total, pl.K_total,
-        pl.listA + 2 * a0, na, pl.Apack);
-    count_launch();
-  }
-  if (do_b && grid_b > 0) {
-    split_kernel<S, BN><<<grid_b, 256, S * B_SLICE_BYTES, st>>>(
-        pl.vb, pl.col_tile, pl.col_local, pl.k_tile, pl.k_local, pl.EB, pl.N_total, pl.K_total,
-        pl.listB, pl.nB, pl.Bpack);
-    count_launch();
+  if (total <= 0 || njobs <= 0) return;
+  const int grid = (int)std::min<int64_t>(total, (int64_t)sm_count * 8);
+  if (a_side)
+    split_kernel<S, BM><<<grid, 256, S * A_SLICE_BYTES, st>>>(d_jobs, njobs, total);
+  else
+    split_kernel<S, BN><<<grid, 256, S * B_SLICE_BYTES, st>>>(d_jobs, njobs, total);
+  count_launch();
+}
+
+// Splits of a table of jobs of one side (A: 128-row bricks, B: 64-column).
+void launch_split(int S, const SplitJob* d_jobs, int njobs, int64_t total, bool a_side,
+                  int sm_count, cudaStream_t st) {
+  switch (S) {
+    case 2: launch_split_t<2>(d_jobs, njobs, total, a_side, sm_count, st); break;
+    case 3: launch_split_t<3>(d_jobs, njobs, total, a_side, sm_count, st); break;
+    case 4: launch_split_t<4>(d_jobs, njobs, total, a_side, sm_count, st); break;
+    case 5: launch_split_t<5>(d_jobs, njobs, total, a_side, sm_count, st); break;
+    default: launch_split_t<6>(d_jobs, njobs, total, a_side, sm_count, st); break;
   }
 }
 
-void launch_split(const OzakiPlan& pl, int sm_count, cudaStream_t st, bool do_a, int64_t a0,
-                  int64_t a1, bool do_b) {
-  switch (pl.S) {
-    case 2: launch_split_t<2>(pl, sm_count, st, do_a, a0, a1, do_b); break;
-    case 3: launch_split_t<3>(pl, sm_count, st, do_a, a0, a1, do_b); break;
-    case 4: launch_split_t<4>(pl, sm_count, st, do_a, a0, a1, do_b); break;
-    case 5: launch_split_t<5>(pl, sm_count, st, do_a, a0, a1, do_b); break;
-    default: launch_split_t<6>(pl, sm_count, st, do_a, a0, a1, do_b); break;
-  }
+// Frames of a table of jobs; max_rows: tallest row tile over the jobs.
+void launch_frames(const FrameJob* d_jobs, int njobs, int64_t tiles, int64_t max_rows,
+                   cudaStream_t s) {
+  if (tiles <= 0 || max_rows <= 0 || njobs <= 0) return;
+  const dim3 g((unsigned)tiles,
+               (unsigned)std::min<int64_t>(65535, (max_rows + kFrameRows - 1) / kFrameRows));
+  frame_kernel<<<g, 256, 0, s>>>(d_jobs, njobs);
+  count_launch();
 }
 
 void index_maps(const int32_t* sz, int64_t n, std::vector<int32_t>& tile,
@@ -1051,12 +1225,12 @@ void index_maps(const int32_t* sz, int64_t n, std::vector<int32_t>& tile,
 
 }  // namespace
 
-// Scheduling order of the output blocks.
-// Blocks are sorted by row chunk, then by super-tiles of gr row blocks x gc
-// column blocks (with 152 CTAs, 8 x 19 is one wave), so CTAs running together
-// share A bricks (gc ways) and B bricks (gr ways) in L2.  Results do not
-// depend on the schedule: the order of every block's sums is fixed by its
-// own k blocks.
+// Scheduling order of the units (pairs of output blocks).
+// Units are sorted by row chunk, then by super-tiles of gr row blocks x gc
+// column-block pairs (with 76 clusters, 4 x 19 is one wave), so clusters
+// running together share A bricks (gc ways, on top of the pair's multicast)
+// and B bricks (gr ways) in L2.  Results do not depend on the schedule: the
+// order of every block's sums is fixed by its own unit's k list.
 tagpu_status ozaki_schedule(OzakiPlan* pl, int gr, int gc, std::string* err) {
   if (gr < 1 || gc < 1) {
     *err = "bad emulated-form schedule";
@@ -1067,7 +1241,7 @@ tagpu_status ozaki_schedule(OzakiPlan* pl, int gr, int gc, std::string* err) {
   pl->tune_gc = gc;
   const auto& hb = pl->h_blk;
   const auto& ho = pl->h_off;
-  const int64_t nsc = (pl->CB + gc - 1) / gc;
+  const int64_t nsc = ((pl->CB + 1) / 2 + gc - 1) / gc;   // super-tile columns (pairs)
   const auto& crb = pl->chunk_rb;
   auto chunk_of = [&](int64_t rb) {
     return (int64_t)(std::upper_bound(crb.begin(), crb.end(), rb) - crb.begin()) - 1;
@@ -1137,6 +1311,8 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   pl->S = slices;
   std::vector<int32_t> rt, rl, rs, kt_, kl, ks, ct, cl, cs;
   index_maps(h_msz, v.Mt, rt, rl, rs);
+  for (int64_t i = 0; i < v.Mt; ++i) pl->max_rows_a = std::max<int64_t>(pl->max_rows_a, h_msz[i]);
+  for (int64_t j = 0; j < v.Nt; ++j) pl->max_rows_b = std::max<int64_t>(pl->max_rows_b, h_nsz[j]);
   index_maps(h_ksz, v.Kt, kt_, kl, ks);
   index_maps(h_nsz, v.Nt, ct, cl, cs);
   pl->M_total = (int64_t)rt.size();
@@ -1223,8 +1399,9 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
       for (int64_t kb = 0; kb < pl->KB; ++kb) t[kb * pl->CB + cb] = h[cb * pl->KB + kb];
     cudaMemcpyAsync(pl->brickB, t.data(), nfb * 4, cudaMemcpyHostToDevice, s);
   }
-  // output blocks and their k-block lists
-  const int64_t nob = pl->RB * pl->CB;
+  // units (pairs of output blocks) and their k-block lists
+  const int64_t CP = (pl->CB + 1) / 2;
+  const int64_t nob = pl->RB * CP;
   int64_t *counts = nullptr, *scan_c = nullptr, *bflag = nullptr, *scan_b = nullptr;
   if ((st = pl->alloc(&counts, nob, err)) || (st = pl->alloc(&scan_c, nob + 1, err)) ||
       (st = pl->alloc(&bflag, nob, err)) || (st = pl->alloc(&scan_b, nob + 1, err)))
@@ -1248,7 +1425,7 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
       pl->brickA, pl->brickB, pl->row_tile, pl->col_tile, v.coff, v.Nt, pl->M_total, pl->N_total,
       pl->RB, pl->CB, pl->KB, scan_c, counts, pl->blk_kb);
   count_launch();
-  block_list_kernel<<<blocks_for(nob, 256), 256, 0, s>>>(counts, scan_b, nob, pl->CB, pl->blk);
+  block_list_kernel<<<blocks_for(nob, 256), 256, 0, s>>>(counts, scan_b, nob, CP, pl->blk);
   count_launch();
   gather_offsets_kernel<<<blocks_for(nob, 256), 256, 0, s>>>(counts, scan_c, scan_b, nob,
                                                              pl->blk_off);
@@ -1257,6 +1434,7 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   if (pl->nblk) {
     slot_pairs_kernel<<<blocks_for(pl->nblk * 32, 256), 256, 0, s>>>(
         pl->blk, pl->blk_off, pl->nblk, pl->blk_kb, pl->brickA, pl->brickB, pl->KB, pl->CB,
+        pl->row_tile, pl->col_tile, v.coff, v.Nt, pl->M_total, pl->N_total, (int32_t)pl->nB,
         pl->blk_ab);
     count_launch();
   }
@@ -1304,8 +1482,11 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   for (int c = 0; c < pl->nchunk; ++c)
     max_slots = std::max(max_slots, pl->chunk_slot[c + 1] - pl->chunk_slot[c]);
   if ((st = pl->alloc(&pl->Apack, a_brick * max_slots, err)) ||
-      (st = pl->alloc(&pl->Bpack, b_brick * pl->nB, err)))
+      (st = pl->alloc(&pl->Bpack, b_brick * (pl->nB + 1), err)))
     return st;
+  // brick nB: all digits zero, read by a unit's column block where it has no
+  // B brick of its own
+  cudaMemsetAsync(pl->Bpack + b_brick * pl->nB, 0, b_brick, s);
   cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) {
     *err = std::string("ozaki planning: ") + cudaGetErrorString(ce);
@@ -1343,6 +1524,25 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   if ((st = pl->alloc(&pl->d_params, 1, err)) || (st = pl->alloc(&pl->d_vstart, 2, err)))
     return st;
   if ((st = ozaki_schedule(pl.get(), pl->tune_gr, pl->tune_gc, err))) return st;
+  // work tables of the frame and split launches
+  pl->h_frames[0] = FrameJob{pl->va, pl->rstart, pl->EA, 0};
+  pl->h_frames[1] = FrameJob{pl->vb, pl->cstart, pl->EB, pl->va.rowt * pl->va.kt};
+  pl->h_split_b = SplitJob{pl->vb,     pl->col_tile, pl->col_local, pl->k_tile,
+                           pl->k_local, pl->EB,      pl->N_total,   pl->K_total,
+                           pl->listB,  pl->nB,      pl->Bpack,     0};
+  pl->h_split_a.clear();
+  for (int c = 0; c < pl->nchunk; ++c)
+    pl->h_split_a.push_back(SplitJob{pl->va, pl->row_tile, pl->row_local, pl->k_tile,
+                                     pl->k_local, pl->EA, pl->M_total, pl->K_total,
+                                     pl->listA + 2 * pl->chunk_slot[c],
+                                     pl->chunk_slot[c + 1] - pl->chunk_slot[c], pl->Apack, 0});
+  {
+    const std::vector<FrameJob> fj(pl->h_frames, pl->h_frames + 2);
+    const std::vector<SplitJob> sb(1, pl->h_split_b);
+    if ((st = pl->upload(&pl->d_frames, fj, err)) || (st = pl->upload(&pl->d_split_b, sb, err)) ||
+        (st = pl->upload(&pl->d_split_a, pl->h_split_a, err)))
+      return st;
+  }
   *out = pl.release();
   return TAGPU_OK;
 }
@@ -1352,17 +1552,11 @@ void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s) {
   cudaMemsetAsync(pl->EA, 0, pl->M_total * 4, s);
   cudaMemsetAsync(pl->EB, 0, pl->N_total * 4, s);
   cudaMemsetAsync(pl->err, 0, 4, s);
-  const int64_t ta = pl->va.rowt * pl->va.kt, tb = pl->vb.rowt * pl->vb.kt;
-  if (ta > 0) {
-    frame_kernel<<<(unsigned)ta, 256, 0, s>>>(pl->va, pl->rstart, pl->EA);
-    count_launch();
-  }
-  if (tb > 0) {
-    frame_kernel<<<(unsigned)tb, 256, 0, s>>>(pl->vb, pl->cstart, pl->EB);
-    count_launch();
-  }
+  launch_frames(pl->d_frames, 2, pl->va.rowt * pl->va.kt + pl->vb.rowt * pl->vb.kt,
+                std::max(pl->max_rows_a, pl->max_rows_b), s);
+  launch_split(pl->S, pl->d_split_b, 1, pl->nB, false, sm_count, s);
   // chunked plans split A chunk by chunk inside ozaki_enqueue_gemm
-  launch_split(*pl, sm_count, s, pl->nchunk == 1, 0, pl->nA, true);
+  if (pl->nchunk == 1) launch_split(pl->S, pl->d_split_a, 1, pl->nA, true, sm_count, s);
 }
 
 void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int nviews,
@@ -1385,13 +1579,71 @@ void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s) {
     return;
   }
   for (int c = 0; c < pl->nchunk; ++c) {
-    launch_split(*pl, sm_count, s, true, pl->chunk_slot[c], pl->chunk_slot[c + 1], false);
+    launch_split(pl->S, pl->d_split_a + c, 1, pl->h_split_a[c].nbricks, true, sm_count, s);
     ozaki_enqueue_gemm_views(pl->d_chunk_params + c, pl->d_chunk_vstart + 2 * c, 1,
                              pl->chunk_blk[c + 1] - pl->chunk_blk[c], pl->S, pl->err, sm_count, s);
   }
 }
 
 int ozaki_chunks(const OzakiPlan* pl) { return pl->nchunk; }
+
+namespace {
+template <typename T>
+void append_bytes(std::vector<uint8_t>* out, const T& x) {
+  const uint8_t* p = reinterpret_cast<const uint8_t*>(&x);
+  out->insert(out->end(), p, p + sizeof(T));
+}
+}  // namespace
+
+void ozaki_group_tables(OzakiPlan* const* pls, int n, std::vector<uint8_t>* zero_jobs,
+                        std::vector<uint8_t>* frame_jobs, std::vector<uint8_t>* split_a,
+                        std::vector<uint8_t>* split_b, OzGroupDims* d) {
+  zero_jobs->clear();
+  frame_jobs->clear();
+  split_a->clear();
+  split_b->clear();
+  *d = OzGroupDims{};
+  for (int i = 0; i < n; ++i) {
+    OzakiPlan* pl = pls[i];
+    append_bytes(zero_jobs, ZeroJob{pl->EA, pl->M_total});
+    append_bytes(zero_jobs, ZeroJob{pl->EB, pl->N_total});
+    append_bytes(zero_jobs, ZeroJob{pl->err, 1});
+    d->nzero += 3;
+    for (int x = 0; x < 2; ++x) {
+      FrameJob f = pl->h_frames[x];
+      f.tile0 = d->frame_tiles;
+      d->frame_tiles += f.v.rowt * f.v.kt;
+      append_bytes(frame_jobs, f);
+      ++d->nframe;
+    }
+    d->frame_rows = std::max({d->frame_rows, pl->max_rows_a, pl->max_rows_b});
+    SplitJob a = pl->h_split_a[0];
+    a.brick0 = d->split_a_bricks;
+    d->split_a_bricks += a.nbricks;
+    append_bytes(split_a, a);
+    ++d->nsplit_a;
+    SplitJob b = pl->h_split_b;
+    b.brick0 = d->split_b_bricks;
+    d->split_b_bricks += b.nbricks;
+    append_bytes(split_b, b);
+    ++d->nsplit_b;
+  }
+}
+
+void ozaki_group_enqueue(const void* zero_jobs, const void* frame_jobs, const void* split_a,
+                         const void* split_b, const OzGroupDims& d, int S, int sm_count,
+                         cudaStream_t s) {
+  if (d.nzero > 0) {
+    zero_kernel<<<(unsigned)d.nzero, 256, 0, s>>>(static_cast<const ZeroJob*>(zero_jobs));
+    count_launch();
+  }
+  launch_frames(static_cast<const FrameJob*>(frame_jobs), d.nframe, d.frame_tiles, d.frame_rows,
+                s);
+  launch_split(S, static_cast<const SplitJob*>(split_b), d.nsplit_b, d.split_b_bricks, false,
+               sm_count, s);
+  launch_split(S, static_cast<const SplitJob*>(split_a), d.nsplit_a, d.split_a_bricks, true,
+               sm_count, s);
+}
 
 // Autotuner: times the schedules of the emulated GEMM on the contraction
 // itself (frames and digit bricks built once), keeps the fastest, and caches
@@ -1432,7 +1684,7 @@ tagpu_status ozaki_autotune(OzakiPlan* pl, int sm_count, cudaStream_t s, const c
     }
   }
   ozaki_enqueue(pl, sm_count, s);  // frames and bricks for the timing runs
-  const int shapes[][2] = {{8, 19}, {4, 38}, {16, 9}, {2, 76}, {1, 152}};
+  const int shapes[][2] = {{4, 19}, {2, 38}, {8, 10}, {1, 76}, {19, 4}};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -1489,7 +1741,7 @@ int ozaki_error(OzakiPlan* pl) {
 }
 
 size_t ozaki_scratch_bytes(const OzakiPlan* pl) { return pl->bytes; }
-int64_t ozaki_blocks(const OzakiPlan* pl) { return pl->nblk; }
+int64_t ozaki_units(const OzakiPlan* pl) { return pl->nblk; }
 void ozaki_destroy(OzakiPlan* pl) { delete pl; }
 
 }  // namespace tagpu

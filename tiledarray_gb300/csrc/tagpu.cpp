@@ -1344,7 +1344,7 @@ tagpu_status plan_all(Contraction& c, const char* c_idx, double alpha, tagpu_arr
     if (ctx->budget && ctx->used.load() > ctx->budget)
       return fail(ctx, TAGPU_ERR_NOMEM, "emulated-form scratch (%zu bytes) exceeds the budget",
                   c.oz_bytes);
-    c.st.gemm_blocks = ozaki_blocks(c.oz);
+    c.st.gemm_blocks = 2 * ozaki_units(c.oz);   // a unit is a pair of output blocks
   } else {
     if ((e = build_dmma_items(c, 0))) return e;
   }
@@ -1397,10 +1397,23 @@ struct LaunchBufs {
   DBuf views, items;            // DMMA contraction views and 64x64 work items
   DBuf ozp[8], ozv[8];          // emulated form: parameter blocks, block offsets
   int64_t oz_nblk[8] = {0};
+  // emulated form, per digit count: job tables of the grouped zeroing,
+  // frame and split launches
+  DBuf gz[8], gf[8], gsa[8], gsb[8];
+  OzGroupDims gdims[8];
+  // plans whose error flag an emulated GEMM launch of this set writes (a
+  // grouped launch writes its first plan's flag for all of its views)
+  std::vector<OzakiPlan*> err_owners;
+  bool any_error() const {
+    for (OzakiPlan* p : err_owners)
+      if (ozaki_error(p)) return true;
+    return false;
+  }
   explicit LaunchBufs(tagpu_ctx* c) : views(c), items(c) {
     for (int i = 0; i < 8; ++i) {
       ozp[i].ctx = c;
       ozv[i].ctx = c;
+      gz[i].ctx = gf[i].ctx = gsa[i].ctx = gsb[i].ctx = c;
     }
   }
 };
@@ -1433,12 +1446,36 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, Launch
   }
   // emulated form: frames and splitting per contraction, then one GEMM launch
   // per slice count over the output blocks of all of them
+  lb.err_owners.clear();
   std::vector<Contraction*> by_s[8];
   for (auto* c : cs) {
     if (!c->emulated()) continue;
-    ozaki_enqueue(c->oz, ctx->sm_count, stream);
     by_s[ozaki_slices(c->oz)].push_back(c);
     c->st.gemm_launches = 5;
+  }
+  // frames and splits: row-chunked plans and lone plans on their own, the
+  // rest of each digit count in one launch per step
+  for (int S = 2; S < 8; ++S) {
+    std::vector<OzakiPlan*> grp;
+    for (auto* c : by_s[S]) {
+      if (ozaki_chunks(c->oz) > 1)
+        ozaki_enqueue(c->oz, ctx->sm_count, stream);
+      else
+        grp.push_back(c->oz);
+    }
+    if (grp.size() == 1) ozaki_enqueue(grp[0], ctx->sm_count, stream);
+    if (grp.size() < 2) continue;
+    if (upload) {
+      std::vector<uint8_t> z, f, a, b;
+      ozaki_group_tables(grp.data(), (int)grp.size(), &z, &f, &a, &b, &lb.gdims[S]);
+      tagpu_status e;
+      if ((e = upload_vec(ctx, lb.gz[S], z)) || (e = upload_vec(ctx, lb.gf[S], f)) ||
+          (e = upload_vec(ctx, lb.gsa[S], a)) || (e = upload_vec(ctx, lb.gsb[S], b)))
+        return e;
+      if (stream != ctx->stream) CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    ozaki_group_enqueue(lb.gz[S].p, lb.gf[S].p, lb.gsa[S].p, lb.gsb[S].p, lb.gdims[S], S,
+                        ctx->sm_count, stream);
   }
   for (int S = 2; S < 8; ++S) {
     auto& g0 = by_s[S];
@@ -1446,11 +1483,13 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, Launch
     for (auto* c : g0) {
       if (ozaki_chunks(c->oz) > 1) {
         ozaki_enqueue_gemm(c->oz, ctx->sm_count, stream);
+        lb.err_owners.push_back(c->oz);
       } else {
         g.push_back(c);
       }
     }
     if (g.empty()) continue;
+    lb.err_owners.push_back(g[0]->oz);
     if (g.size() == 1) {
       ozaki_enqueue_gemm(g[0]->oz, ctx->sm_count, stream);
       continue;
@@ -1461,7 +1500,7 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, Launch
       std::vector<int64_t> vstart(1, 0);
       for (size_t i = 0; i < g.size(); ++i) {
         ozaki_params(g[i]->oz, params.data() + i * psz);
-        vstart.push_back(vstart.back() + ozaki_blocks(g[i]->oz));
+        vstart.push_back(vstart.back() + ozaki_units(g[i]->oz));
       }
       tagpu_status e;
       if ((e = upload_vec(ctx, lb.ozp[S], params)) || (e = upload_vec(ctx, lb.ozv[S], vstart)))
@@ -1700,9 +1739,8 @@ tagpu_status tagpu_batch_run(tagpu_batch* b) {
     // run once eagerly (uploads the work lists), then capture the launches
     if ((e = enqueue_gemms(ctx, cs, b->lb, true))) return e;
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    for (auto* c : cs)
-      if (c->emulated() && ozaki_error(c->oz))
-        return fail(ctx, TAGPU_ERR_TIMEOUT, "emulated GEMM: a bounded wait ran out");
+    if (b->lb.any_error())
+      return fail(ctx, TAGPU_ERR_TIMEOUT, "emulated GEMM: a bounded wait ran out");
     CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     e = enqueue_gemms(ctx, cs, b->lb, false);
     cudaGraph_t g = nullptr;
@@ -1721,9 +1759,8 @@ tagpu_status tagpu_batch_run(tagpu_batch* b) {
   } else {
     CUDA_TRY(ctx, cudaGraphLaunch(b->exec, ctx->stream));
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    for (auto& en : b->entries)
-      if (en.plan->emulated() && ozaki_error(en.plan->oz))
-        return fail(ctx, TAGPU_ERR_TIMEOUT, "emulated GEMM: a bounded wait ran out");
+    if (b->lb.any_error())
+      return fail(ctx, TAGPU_ERR_TIMEOUT, "emulated GEMM: a bounded wait ran out");
   }
   tagpu_contract_stats& s = b->stats;
   s = tagpu_contract_stats{};
@@ -1981,17 +2018,19 @@ size_t footprint_bound(tagpu_array* A, const std::vector<std::string>& ai, tagpu
 void tagpu_server::run() {
   std::vector<std::shared_ptr<Req>> inflight;  // GEMMs enqueued on gemm_stream
   LaunchBufs lb_a(ctx), lb_b(ctx);
+  LaunchBufs* inflight_lb = nullptr;   // the buffers of the batch in flight
   bool use_a = true;
   auto finish_inflight = [&]() {
     if (inflight.empty()) return;
     cudaError_t ce = cudaStreamSynchronize(gemm_stream);
+    // a bounded wait that ran out in a grouped launch invalidates its batch
+    const bool timed_out = ce == cudaSuccess && inflight_lb && inflight_lb->any_error();
     const double t = now_ms();
     std::lock_guard<std::mutex> lk(m);
     for (auto& r : inflight) {
       Contraction& c = *r->plan;
       r->res.status = ce == cudaSuccess ? TAGPU_OK : TAGPU_ERR_CUDA;
-      if (r->res.status == TAGPU_OK && c.emulated() && ozaki_error(c.oz))
-        r->res.status = TAGPU_ERR_TIMEOUT;
+      if (r->res.status == TAGPU_OK && timed_out) r->res.status = TAGPU_ERR_TIMEOUT;
       if (r->res.status == TAGPU_OK) {
         fill_stats(c);
         r->C = c.Cfinal ? c.Cfinal.release() : c.C.release();
@@ -2066,6 +2105,7 @@ void tagpu_server::run() {
       LaunchBufs& lb = use_a ? lb_a : lb_b;
       use_a = !use_a;
       tagpu_status e = enqueue_gemms(ctx, cs, lb, true, gemm_stream);
+      inflight_lb = &lb;
       const uint64_t bid = next_batch++;
       for (auto& r : ok) {
         r->res.batch_size = (int)ok.size();
