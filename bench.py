@@ -639,14 +639,14 @@ def main():
         del Cp, x, y
     # end to end through the public API with host buffers
     if rank == 0 and not args.no_e2e:
-        import torch
-        a_host = torch.empty(A.info().elements, dtype=torch.float64, pin_memory=True).numpy()
-        b_host = torch.empty(B.info().elements, dtype=torch.float64, pin_memory=True).numpy()
+        # pinned host buffers from the library (tagpu_host_alloc)
+        a_host = w.host_array(A.info().elements)
+        b_host = w.host_array(B.info().elements)
         a_host[:] = A.download()
         b_host[:] = B.download()
         c_host = None
         C2, _ = step()   # the result's pinned host buffer is allocated outside the timing
-        c_host = torch.empty(C2.info().elements, dtype=torch.float64, pin_memory=True).numpy()
+        c_host = w.host_array(C2.info().elements)
         del C2
         e2e_ms, parts = [], []
         for _ in range(max(1, min(args.steps, 3))):

@@ -131,6 +131,24 @@ tagpu_status tagpu_array_generate(tagpu_array* a, uint64_t seed, uint64_t stream
                                   int kind, const double* tile_scale,
                                   int compute_shape, float threshold);
 
+/* Pinned host buffers for staging operands and results (no counterpart in
+ * the reference, whose tiles live in host memory).  Copies between device
+ * arrays and these buffers run at the host link's full rate every time; some
+ * other pinned allocators on this platform slow down after other large
+ * transfers.  Free with tagpu_host_free. */
+tagpu_status tagpu_host_alloc(tagpu_ctx* ctx, size_t bytes, void** p);
+tagpu_status tagpu_host_free(tagpu_ctx* ctx, void* p);
+
+/* Archive I/O: DistArray::serialize (dist_array.h:1583-1592, store) and its
+ * input form (:1603-1645, load) for a single-rank world, in that order: type
+ * tag, world size and rank, TiledRange, shape, stored-tile count, then each
+ * stored tile's range and row-major data.  Fixed-width little-endian fields
+ * (the layout is written out in tiledarray_gb300/csrc/tagpu.cpp); tiles stream
+ * through a pinned staging buffer.  A file that is not such an archive, or
+ * whose tiles do not match its shape, is TAGPU_ERR_INVALID. */
+tagpu_status tagpu_array_save(const tagpu_array* a, const char* path);
+tagpu_status tagpu_array_load(tagpu_ctx* ctx, const char* path, tagpu_array** a);
+
 /* TiledArray::truncate (conversions/truncate.h:52-80): the shape is rebuilt
  * from the Frobenius norms of the stored tiles (computed on the device in
  * storage order, as Tensor::norm), scaled by tile volume, with `threshold`

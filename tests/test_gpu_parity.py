@@ -293,3 +293,48 @@ def test_contract_accumulate(ta, world, precision):
         want = c + p if (c is not None and p is not None) else (c if c is not None else p)
         assert np.array_equal(r_d[r_off[t]:r_off[t] + vol], want)
     assert set(np.flatnonzero(r_off >= 0)) == set(np.flatnonzero(exp_n > 0))
+
+
+@pytest.mark.parametrize("sparse", [True, False])
+def test_archive_roundtrip(ta, world, tmp_path, sparse):
+    """save then load gives the same tiling, shape, offsets and tile data bit
+    for bit; a file that is not an archive, or a truncated one, is rejected."""
+    h1, h2 = uneven_hashmarks(500, 30, 140, 15), uneven_hashmarks(300, 20, 90, 16)
+    if sparse:
+        keep = (np.arange((len(h1) - 1) * (len(h2) - 1)) % 3) != 0
+        A, tr = gpu_operand(ta, world, [h1, h2], 17, 0, kind=0, keep=keep)
+    else:
+        A = ta.DistArray(world, ta.TiledRange([h1, h2]))
+        A.generate(17, 0, 0, None, False)
+    path = tmp_path / "a.tagpu"
+    A.save(path)
+    B = ta.DistArray.load(world, path)
+    ia, ib = A.info(), B.info()
+    assert (ia.dense, ia.elements, ia.zero_tiles) == (ib.dense, ib.elements, ib.zero_tiles)
+    assert B.trange.dims == A.trange.dims
+    assert np.array_equal(A.tile_offsets(), B.tile_offsets())
+    assert np.array_equal(A.norms(), B.norms())
+    assert np.array_equal(A.download(), B.download())
+    bad = tmp_path / "bad.tagpu"
+    bad.write_bytes(b"not an archive at all")
+    with pytest.raises(ta.TAGPUError) as e:
+        ta.DistArray.load(world, bad)
+    assert e.value.status == 1
+    cut = tmp_path / "cut.tagpu"
+    cut.write_bytes(path.read_bytes()[:-100])
+    with pytest.raises(ta.TAGPUError):
+        ta.DistArray.load(world, cut)
+
+
+def test_host_buffers_roundtrip(ta, world):
+    """Library-owned pinned host buffers carry an array's tiles both ways."""
+    A, _ = gpu_operand(ta, world, [[0, 40, 100], [0, 64, 90]], 3, 0, kind=0)
+    n = A.info().elements
+    buf = world.host_array(n)
+    buf[:] = A.download()
+    B = ta.DistArray(world, A.trange)
+    B.set_shape(A.norms(), do_not_scale=True, threshold=A.info().threshold)
+    B.upload(buf)
+    out = world.host_array(n)
+    world.check(world.L.tagpu_array_download(B.h, out.ctypes.data_as(ta._f64p), n))
+    assert np.array_equal(out, A.download())

@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 
 import numpy as np
 
@@ -137,6 +138,10 @@ SIGNATURES = {
     "tagpu_array_get_tile_offsets": (ctypes.c_int, [_vp, _i64p]),
     "tagpu_array_get_tile": (ctypes.c_int, [_vp, ctypes.c_int64, _f64p, ctypes.c_int64]),
     "tagpu_array_truncate": (ctypes.c_int, [_vp, ctypes.c_float]),
+    "tagpu_array_save": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+    "tagpu_host_alloc": (ctypes.c_int, [_vp, ctypes.c_size_t, ctypes.POINTER(_vp)]),
+    "tagpu_host_free": (ctypes.c_int, [_vp, _vp]),
+    "tagpu_array_load": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_vp)]),
     "tagpu_contract_accumulate": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, _vp,
                                                  ctypes.c_char_p, _vp, ctypes.c_char_p, _vp,
                                                  _vp]),
@@ -238,6 +243,18 @@ class World:
         ms = ctypes.c_double(0)
         self.check(self.L.tagpu_timer_stop(self.h, ctypes.byref(ms)))
         return ms.value
+
+    def host_array(self, n, dtype=np.float64):
+        """A numpy array of n elements in pinned host memory owned by the
+        library (tagpu_host_alloc), freed when the array is collected."""
+        dt = np.dtype(dtype)
+        p = _vp()
+        self.check(self.L.tagpu_host_alloc(self.h, max(1, n) * dt.itemsize, ctypes.byref(p)))
+        buf = (ctypes.c_char * (max(1, n) * dt.itemsize)).from_address(p.value)
+        arr = np.frombuffer(buf, dtype=dt, count=n)
+        # the buffer outlives every array and view made from it
+        weakref.finalize(buf, self.L.tagpu_host_free, self.h, p)
+        return arr
 
     def last_stats(self):
         s = ContractStats()
@@ -487,6 +504,17 @@ class DistArray:
         self.world.check(self.world.L.tagpu_array_generate(
             self.h, int(seed), int(stream), int(kind), None if ts is None else _p(ts, _f64p),
             int(compute_shape), np.float32(threshold)))
+
+    def save(self, path):
+        """Archive of the array (DistArray::serialize order, single rank)."""
+        self.world.check(self.world.L.tagpu_array_save(self.h, os.fsencode(path)))
+
+    @staticmethod
+    def load(world, path):
+        """An array read back from tagpu_array_save's archive."""
+        h = _vp()
+        world.check(world.L.tagpu_array_load(world.h, os.fsencode(path), ctypes.byref(h)))
+        return DistArray(world, _handle=h)
 
     def truncate(self, threshold=-1.0):
         """TiledArray::truncate: shape from the stored tiles' norms, small tiles dropped."""

@@ -148,7 +148,7 @@ size_t ozaki_scratch_bytes(const OzakiPlan* pl);
 // to upload as they are), the enqueue runs zeroing, frames, B and A splits.
 struct OzGroupDims {
   int nzero = 0, nframe = 0, nsplit_a = 0, nsplit_b = 0;
-  int64_t frame_tiles = 0, frame_rows = 0, split_a_bricks = 0, split_b_bricks = 0;
+  int64_t frame_items = 0, split_a_bricks = 0, split_b_bricks = 0;
 };
 void ozaki_group_tables(OzakiPlan* const* pls, int n, std::vector<uint8_t>* zero_jobs,
                         std::vector<uint8_t>* frame_jobs, std::vector<uint8_t>* split_a,

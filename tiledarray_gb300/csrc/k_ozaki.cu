@@ -349,7 +349,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
       mbar_init(smem_u32(&bar_empty[s]), 2);   // both CTAs' MMAs have read the stage
     }
     mbar_init(smem_u32(&bar_acc_full), 1);
-    for (int t = 0; t <= TOP; ++t) mbar_init(smem_u32(&bar_level[t]), EPI_WARPS * 32);
+    for (int t = 0; t <= TOP; ++t) mbar_init(smem_u32(&bar_level[t]), EPI_WARPS);  // per warp
     mbar_init(smem_u32(&bar_done), 1);
     abort_s = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -626,7 +626,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
           tmem_ld16(lane_addr + (t - 2) * BN + 16, v1);
           tmem_wait_ld();
           tc_fence_before();
-          mbar_arrive(smem_u32(&bar_level[t]));
+          __syncwarp();   // every lane's reads are done: one arrival per warp
+          if (lane == 0) mbar_arrive(smem_u32(&bar_level[t]));
           if (t > kExactTop) {
             // whole-block fp32 sum: integer valued, possibly beyond 2^31
             const int sh = 8 * (TOP - t);
@@ -710,56 +711,63 @@ __device__ __forceinline__ int exp_field(double x) {
   return (int)((__double_as_longlong(x) >> 52) & 0x7ff);
 }
 
-// A frame job: one operand of one contraction.  Tiles of all jobs of a
-// launch are numbered consecutively from each job's tile0.
+// A frame job: one operand of one contraction.  Its work items are
+// (row tile, chunk of kFrameRows rows, k tile), row-chunk major: row tile rt
+// owns chunks [chunk0[rt], chunk0[rt+1]).  Items of all jobs of a launch are
+// numbered consecutively from each job's item0.
+constexpr int kFrameRows = 64;
 struct FrameJob {
   OperandView v;
   const int32_t* row_start;   // first fused row of every row tile
+  const int32_t* chunk0;      // rowt + 1 entries
   int32_t* E;                 // frames of the operand's fused rows
-  int64_t tile0;
+  int64_t item0;
 };
 
 // Frames: max biased exponent of every operand row over its k, folded into
-// the row's frame with atomicMax.  Grid x = operand tile (rt, kt) over all
-// jobs, grid y = chunk of kFrameRows rows of that tile, so long fused rows
-// and tall tiles both spread over many CTAs.  Both storage orders are read
-// coalesced: rows of a row-major tile by warps along k, columns of a
-// transposed tile by threads along the rows.
-constexpr int kFrameRows = 64;
+// the row's frame with atomicMax.  One CTA per work item (64 rows of one
+// operand tile), so long fused rows and tall tiles both spread over many
+// CTAs and no CTA is idle.  Both storage orders are read coalesced: rows of a
+// row-major tile by warps along k, columns of a transposed tile by threads
+// along the rows.
 __global__ void __launch_bounds__(256) frame_kernel(const FrameJob* __restrict__ jobs,
                                                     int njobs) {
+  const int64_t g = blockIdx.x;
   int lo = 0, hi = njobs;
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
-    if (jobs[mid].tile0 <= (int64_t)blockIdx.x) lo = mid; else hi = mid;
+    if (jobs[mid].item0 <= g) lo = mid; else hi = mid;
   }
   const FrameJob& J = jobs[lo];
   const OperandView& v = J.v;
-  const int64_t t = (int64_t)blockIdx.x - J.tile0;   // tile (rt, kt), rt-major
-  if (t >= v.rowt * v.kt) return;
-  const int64_t rt = t / v.kt, ktile = t - (t / v.kt) * v.kt;
+  const int64_t i = g - J.item0;
+  const int64_t q = i / v.kt, ktile = i - q * v.kt;   // q: global row chunk of the job
+  int a = 0, b = (int)v.rowt;                          // row tile owning chunk q
+  while (b - a > 1) {
+    const int mid = (a + b) >> 1;
+    if (J.chunk0[mid] <= q) a = mid; else b = mid;
+  }
+  const int64_t rt = a;
   const int64_t o = v.off[rt * v.off_stride_row + ktile * v.off_stride_k];
   if (o < 0) return;
   const int m = v.rsz[rt], kk = v.ksz[ktile];
+  const int r0 = (int)(q - J.chunk0[rt]) * kFrameRows, r1 = min(m, r0 + kFrameRows);
   const double* base = v.data + o;
   int32_t* Er = J.E + J.row_start[rt];
-  for (int r0 = blockIdx.y * kFrameRows; r0 < m; r0 += gridDim.y * kFrameRows) {
-    const int r1 = min(m, r0 + kFrameRows);
-    if (v.row_contig) {            // element (r, k) at k * m + r
-      const int r = r0 + (threadIdx.x % kFrameRows);
-      const int kq = threadIdx.x / kFrameRows, nq = blockDim.x / kFrameRows;
+  if (v.row_contig) {              // element (r, k) at k * m + r
+    const int r = r0 + (threadIdx.x % kFrameRows);
+    const int kq = threadIdx.x / kFrameRows, nq = blockDim.x / kFrameRows;
+    int e = 0;
+    if (r < r1)
+      for (int k = kq; k < kk; k += nq) e = max(e, exp_field(base[(int64_t)k * m + r]));
+    if (e > 0) atomicMax(&Er[r], e);
+  } else {                         // element (r, k) at r * kk + k
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int r = r0 + warp; r < r1; r += blockDim.x >> 5) {
       int e = 0;
-      if (r < r1)
-        for (int k = kq; k < kk; k += nq) e = max(e, exp_field(base[(int64_t)k * m + r]));
-      if (e > 0) atomicMax(&Er[r], e);
-    } else {                       // element (r, k) at r * kk + k
-      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-      for (int r = r0 + warp; r < r1; r += blockDim.x >> 5) {
-        int e = 0;
-        for (int k = lane; k < kk; k += 32) e = max(e, exp_field(base[(int64_t)r * kk + k]));
-        for (int s = 16; s > 0; s >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, s));
-        if (lane == 0 && e > 0) atomicMax(&Er[r], e);
-      }
+      for (int k = lane; k < kk; k += 32) e = max(e, exp_field(base[(int64_t)r * kk + k]));
+      for (int s = 16; s > 0; s >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, s));
+      if (lane == 0 && e > 0) atomicMax(&Er[r], e);
     }
   }
 }
@@ -1085,7 +1093,9 @@ struct OzakiPlan {
   int32_t *EA = nullptr, *EB = nullptr, *brickA = nullptr, *brickB = nullptr, *listA = nullptr,
           *listB = nullptr, *blk = nullptr, *blk_kb = nullptr;
   int64_t *blk_off = nullptr, *blk_rng = nullptr;
-  int64_t max_rows_a = 0, max_rows_b = 0;   // tallest row tile of each operand
+  // frame work: per row tile the first 64-row chunk (prefix), per operand
+  int32_t *chunk0_a = nullptr, *chunk0_b = nullptr;
+  int64_t frame_items_a = 0, frame_items_b = 0;
   // work tables of the frame and split launches (host copies and device)
   FrameJob h_frames[2];                    // A, B
   SplitJob h_split_b;
@@ -1199,13 +1209,10 @@ void launch_split(int S, const SplitJob* d_jobs, int njobs, int64_t total, bool 
   }
 }
 
-// Frames of a table of jobs; max_rows: tallest row tile over the jobs.
-void launch_frames(const FrameJob* d_jobs, int njobs, int64_t tiles, int64_t max_rows,
-                   cudaStream_t s) {
-  if (tiles <= 0 || max_rows <= 0 || njobs <= 0) return;
-  const dim3 g((unsigned)tiles,
-               (unsigned)std::min<int64_t>(65535, (max_rows + kFrameRows - 1) / kFrameRows));
-  frame_kernel<<<g, 256, 0, s>>>(d_jobs, njobs);
+// Frames of a table of jobs with `items` work items in all.
+void launch_frames(const FrameJob* d_jobs, int njobs, int64_t items, cudaStream_t s) {
+  if (items <= 0 || njobs <= 0) return;
+  frame_kernel<<<(unsigned)items, 256, 0, s>>>(d_jobs, njobs);
   count_launch();
 }
 
@@ -1311,8 +1318,13 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   pl->S = slices;
   std::vector<int32_t> rt, rl, rs, kt_, kl, ks, ct, cl, cs;
   index_maps(h_msz, v.Mt, rt, rl, rs);
-  for (int64_t i = 0; i < v.Mt; ++i) pl->max_rows_a = std::max<int64_t>(pl->max_rows_a, h_msz[i]);
-  for (int64_t j = 0; j < v.Nt; ++j) pl->max_rows_b = std::max<int64_t>(pl->max_rows_b, h_nsz[j]);
+  std::vector<int32_t> c0a(1, 0), c0b(1, 0);
+  for (int64_t i = 0; i < v.Mt; ++i)
+    c0a.push_back(c0a.back() + (h_msz[i] + kFrameRows - 1) / kFrameRows);
+  for (int64_t j = 0; j < v.Nt; ++j)
+    c0b.push_back(c0b.back() + (h_nsz[j] + kFrameRows - 1) / kFrameRows);
+  pl->frame_items_a = (int64_t)c0a.back() * v.Kt;
+  pl->frame_items_b = (int64_t)c0b.back() * v.Kt;
   index_maps(h_ksz, v.Kt, kt_, kl, ks);
   index_maps(h_nsz, v.Nt, ct, cl, cs);
   pl->M_total = (int64_t)rt.size();
@@ -1525,8 +1537,10 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
     return st;
   if ((st = ozaki_schedule(pl.get(), pl->tune_gr, pl->tune_gc, err))) return st;
   // work tables of the frame and split launches
-  pl->h_frames[0] = FrameJob{pl->va, pl->rstart, pl->EA, 0};
-  pl->h_frames[1] = FrameJob{pl->vb, pl->cstart, pl->EB, pl->va.rowt * pl->va.kt};
+  if ((st = pl->upload(&pl->chunk0_a, c0a, err)) || (st = pl->upload(&pl->chunk0_b, c0b, err)))
+    return st;
+  pl->h_frames[0] = FrameJob{pl->va, pl->rstart, pl->chunk0_a, pl->EA, 0};
+  pl->h_frames[1] = FrameJob{pl->vb, pl->cstart, pl->chunk0_b, pl->EB, pl->frame_items_a};
   pl->h_split_b = SplitJob{pl->vb,     pl->col_tile, pl->col_local, pl->k_tile,
                            pl->k_local, pl->EB,      pl->N_total,   pl->K_total,
                            pl->listB,  pl->nB,      pl->Bpack,     0};
@@ -1552,8 +1566,7 @@ void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s) {
   cudaMemsetAsync(pl->EA, 0, pl->M_total * 4, s);
   cudaMemsetAsync(pl->EB, 0, pl->N_total * 4, s);
   cudaMemsetAsync(pl->err, 0, 4, s);
-  launch_frames(pl->d_frames, 2, pl->va.rowt * pl->va.kt + pl->vb.rowt * pl->vb.kt,
-                std::max(pl->max_rows_a, pl->max_rows_b), s);
+  launch_frames(pl->d_frames, 2, pl->frame_items_a + pl->frame_items_b, s);
   launch_split(pl->S, pl->d_split_b, 1, pl->nB, false, sm_count, s);
   // chunked plans split A chunk by chunk inside ozaki_enqueue_gemm
   if (pl->nchunk == 1) launch_split(pl->S, pl->d_split_a, 1, pl->nA, true, sm_count, s);
@@ -1611,12 +1624,11 @@ void ozaki_group_tables(OzakiPlan* const* pls, int n, std::vector<uint8_t>* zero
     d->nzero += 3;
     for (int x = 0; x < 2; ++x) {
       FrameJob f = pl->h_frames[x];
-      f.tile0 = d->frame_tiles;
-      d->frame_tiles += f.v.rowt * f.v.kt;
+      f.item0 = d->frame_items;
+      d->frame_items += x == 0 ? pl->frame_items_a : pl->frame_items_b;
       append_bytes(frame_jobs, f);
       ++d->nframe;
     }
-    d->frame_rows = std::max({d->frame_rows, pl->max_rows_a, pl->max_rows_b});
     SplitJob a = pl->h_split_a[0];
     a.brick0 = d->split_a_bricks;
     d->split_a_bricks += a.nbricks;
@@ -1637,8 +1649,7 @@ void ozaki_group_enqueue(const void* zero_jobs, const void* frame_jobs, const vo
     zero_kernel<<<(unsigned)d.nzero, 256, 0, s>>>(static_cast<const ZeroJob*>(zero_jobs));
     count_launch();
   }
-  launch_frames(static_cast<const FrameJob*>(frame_jobs), d.nframe, d.frame_tiles, d.frame_rows,
-                s);
+  launch_frames(static_cast<const FrameJob*>(frame_jobs), d.nframe, d.frame_items, s);
   launch_split(S, static_cast<const SplitJob*>(split_b), d.nsplit_b, d.split_b_bricks, false,
                sm_count, s);
   launch_split(S, static_cast<const SplitJob*>(split_a), d.nsplit_a, d.split_a_bricks, true,

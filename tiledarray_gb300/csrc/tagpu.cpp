@@ -13,6 +13,7 @@
 // done here (size vectors, scaling) rounds each operation separately, as the
 // CPU reference does.
 #include <cuda_runtime.h>
+#include <sys/mman.h>
 
 #include <algorithm>
 #include <atomic>
@@ -886,6 +887,264 @@ tagpu_status tagpu_array_get_tile(const tagpu_array* a, int64_t ordinal, double*
     CUDA_TRY(ctx, cudaMemcpyAsync(tile, a->data + a->off[ordinal], n * sizeof(double),
                                   cudaMemcpyDeviceToHost, ctx->stream));
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return TAGPU_OK;
+}
+
+// ---- archive I/O ------------------------------------------------------------
+// The order of DistArray::serialize (dist_array.h:1583-1592) with a
+// single-rank world: a type tag, world size and rank, the TiledRange, the
+// shape, the number of stored tiles, then each stored tile (its range and its
+// row-major data) in ordinal order.  Little endian, fixed-width fields:
+//   "TAGPUARR" u32 version=1 | u32 type tag (1 = Tensor<double>)
+//   i64 world size (1) | i64 world rank (0)
+//   u32 rank | per dimension: i64 ntiles, i64 hashmarks[ntiles + 1]
+//   u8 dense | f32 threshold | i64 zero tiles | f32 scaled norms[tiles] (sparse)
+//   i64 stored tiles | per tile: i64 ordinal, i64 lo[rank], i64 hi[rank],
+//                                f64 data[volume]
+// Tiles move through a pinned staging buffer, so arrays larger than host
+// memory stream through.
+}  // extern "C"
+
+namespace {
+struct HostMap {
+  void* base;
+  size_t len;
+  bool mapped;   // mmap + cudaHostRegister (else cudaHostAlloc)
+};
+std::mutex& host_maps_mu() {
+  static std::mutex m;
+  return m;
+}
+std::unordered_map<void*, HostMap>& host_maps() {
+  static std::unordered_map<void*, HostMap> m;
+  return m;
+}
+// Transparent huge page size if the kernel offers them to madvise, else 0.
+size_t host_huge_page() {
+  static size_t sz = [] {
+    size_t v = 0;
+    if (FILE* f = fopen("/sys/kernel/mm/transparent_hugepage/enabled", "r")) {
+      char buf[128] = {0};
+      const size_t n = fread(buf, 1, sizeof(buf) - 1, f);
+      fclose(f);
+      buf[n] = 0;
+      if (!strstr(buf, "[never]")) {
+        if (FILE* g = fopen("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size", "r")) {
+          unsigned long long x = 0;
+          if (fscanf(g, "%llu", &x) == 1 && x >= 4096 && x <= (1ull << 30) && !(x & (x - 1)))
+            v = (size_t)x;
+          fclose(g);
+        }
+      }
+    }
+    return v;
+  }();
+  return sz;
+}
+constexpr char kArchiveMagic[8] = {'T', 'A', 'G', 'P', 'U', 'A', 'R', 'R'};
+constexpr size_t kStage = size_t(64) << 20;
+
+struct PinnedStage {
+  void* p = nullptr;
+  PinnedStage() {
+    if (cudaMallocHost(&p, kStage) != cudaSuccess) p = nullptr;
+  }
+  ~PinnedStage() {
+    if (p) cudaFreeHost(p);
+  }
+};
+
+struct File {
+  FILE* f = nullptr;
+  File(const char* path, const char* mode) : f(fopen(path, mode)) {}
+  ~File() {
+    if (f) fclose(f);
+  }
+  template <typename T>
+  bool put(const T& x) { return fwrite(&x, sizeof(T), 1, f) == 1; }
+  template <typename T>
+  bool get(T& x) { return fread(&x, sizeof(T), 1, f) == 1; }
+};
+}  // namespace
+
+extern "C" {
+
+// Host buffers: an anonymous mapping aligned to the transparent huge page
+// size, advised to use huge pages, touched and registered with CUDA, so the
+// GPU reaches it through few, large translations; cudaHostAlloc where that
+// is not available.  The mapping of each buffer is remembered for the free.
+tagpu_status tagpu_host_alloc(tagpu_ctx* ctx, size_t bytes, void** p) {
+  if (!ctx || !p) return TAGPU_ERR_INVALID;
+  *p = nullptr;
+  cudaSetDevice(ctx->device);
+  if (bytes == 0) return TAGPU_OK;
+  const size_t huge = host_huge_page();
+  if (huge) {
+    const size_t len = (bytes + huge - 1) / huge * huge;
+    void* m = mmap(nullptr, len + huge, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1,
+                   0);
+    if (m != MAP_FAILED) {
+      uint8_t* a = (uint8_t*)(((uintptr_t)m + huge - 1) & ~(uintptr_t)(huge - 1));
+      madvise(a, len, MADV_HUGEPAGE);
+      memset(a, 0, len);
+      if (cudaHostRegister(a, len, cudaHostRegisterDefault) == cudaSuccess) {
+        std::lock_guard<std::mutex> lk(host_maps_mu());
+        host_maps()[a] = HostMap{m, len + huge, true};
+        *p = a;
+        return TAGPU_OK;
+      }
+      cudaGetLastError();
+      munmap(m, len + huge);
+    }
+  }
+  const cudaError_t e = cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return fail(ctx, TAGPU_ERR_NOMEM, "cudaHostAlloc(%zu) failed: %s", bytes,
+                cudaGetErrorString(e));
+  }
+  std::lock_guard<std::mutex> lk(host_maps_mu());
+  host_maps()[*p] = HostMap{*p, bytes, false};
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_host_free(tagpu_ctx* ctx, void* p) {
+  if (!ctx) return TAGPU_ERR_INVALID;
+  if (!p) return TAGPU_OK;
+  HostMap hm{};
+  {
+    std::lock_guard<std::mutex> lk(host_maps_mu());
+    auto it = host_maps().find(p);
+    if (it == host_maps().end())
+      return fail(ctx, TAGPU_ERR_INVALID, "host_free: not a tagpu host buffer");
+    hm = it->second;
+    host_maps().erase(it);
+  }
+  if (hm.mapped) {
+    cudaHostUnregister(p);
+    munmap(hm.base, hm.len);
+  } else {
+    cudaFreeHost(p);
+  }
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_array_save(const tagpu_array* a, const char* path) {
+  if (!a || !path) return TAGPU_ERR_INVALID;
+  tagpu_ctx* ctx = a->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  File out(path, "wb");
+  if (!out.f) return fail(ctx, TAGPU_ERR_INVALID, "save: cannot open %s", path);
+  PinnedStage stage;
+  if (!stage.p) return fail(ctx, TAGPU_ERR_NOMEM, "save: no pinned staging buffer");
+  bool ok = fwrite(kArchiveMagic, 1, 8, out.f) == 8;
+  ok = ok && out.put<uint32_t>(1) && out.put<uint32_t>(1) && out.put<int64_t>(1) &&
+       out.put<int64_t>(0) && out.put<uint32_t>((uint32_t)a->rank);
+  for (int d = 0; d < a->rank && ok; ++d) {
+    ok = out.put<int64_t>(a->nt[d]) &&
+         fwrite(a->hm[d].data(), 8, a->hm[d].size(), out.f) == a->hm[d].size();
+  }
+  const int64_t n = a->ntiles();
+  ok = ok && out.put<uint8_t>(a->dense ? 1 : 0) && out.put<float>(a->threshold) &&
+       out.put<int64_t>(a->zero_count);
+  if (ok && !a->dense) ok = fwrite(a->norms.data(), 4, (size_t)n, out.f) == (size_t)n;
+  int64_t count = 0;
+  for (int64_t t = 0; t < n; ++t) count += a->off[t] >= 0;
+  ok = ok && out.put<int64_t>(count);
+  int64_t idx[8];
+  for (int64_t t = 0; t < n && ok; ++t) {
+    if (a->off[t] < 0) continue;
+    a->tile_index(t, idx);
+    ok = out.put<int64_t>(t);
+    for (int d = 0; d < a->rank && ok; ++d) ok = out.put<int64_t>(a->hm[d][idx[d]]);
+    for (int d = 0; d < a->rank && ok; ++d) ok = out.put<int64_t>(a->hm[d][idx[d] + 1]);
+    const size_t bytes = (size_t)a->tile_volume(t) * sizeof(double);
+    for (size_t x = 0; x < bytes && ok; x += kStage) {
+      const size_t m = std::min(kStage, bytes - x);
+      CUDA_TRY(ctx, cudaMemcpyAsync(stage.p, (const uint8_t*)(a->data + a->off[t]) + x, m,
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+      CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      ok = fwrite(stage.p, 1, m, out.f) == m;
+    }
+  }
+  if (!ok) return fail(ctx, TAGPU_ERR_INVALID, "save: write to %s failed", path);
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_array_load(tagpu_ctx* ctx, const char* path, tagpu_array** out_a) {
+  if (!ctx || !path || !out_a) return TAGPU_ERR_INVALID;
+  *out_a = nullptr;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  File in(path, "rb");
+  if (!in.f) return fail(ctx, TAGPU_ERR_INVALID, "load: cannot open %s", path);
+  auto bad = [&](const char* what) {
+    return fail(ctx, TAGPU_ERR_INVALID, "load: %s: %s", path, what);
+  };
+  char magic[8];
+  uint32_t version = 0, tag = 0, rank = 0;
+  int64_t wsize = 0, wrank = 0;
+  if (fread(magic, 1, 8, in.f) != 8 || memcmp(magic, kArchiveMagic, 8) != 0)
+    return bad("not an array archive");
+  if (!in.get(version) || version != 1) return bad("unknown archive version");
+  if (!in.get(tag) || tag != 1) return bad("tile type is not Tensor<double>");
+  if (!in.get(wsize) || !in.get(wrank) || wsize != 1 || wrank != 0)
+    return bad("archive of another world");
+  if (!in.get(rank) || rank > 8) return bad("bad rank");
+  std::vector<std::vector<int64_t>> hm(rank);
+  for (uint32_t d = 0; d < rank; ++d) {
+    int64_t nt = -1;
+    if (!in.get(nt) || nt < 0 || nt > (int64_t(1) << 32)) return bad("bad tile count");
+    hm[d].resize((size_t)nt + 1);
+    if (fread(hm[d].data(), 8, hm[d].size(), in.f) != hm[d].size()) return bad("truncated");
+    for (int64_t i = 0; i < nt; ++i)
+      if (hm[d][i + 1] < hm[d][i]) return bad("hashmarks decrease");
+  }
+  std::unique_ptr<tagpu_array> a(new_array(ctx, hm));
+  uint8_t dense = 1;
+  float thr = 0.0f;
+  int64_t zeros = 0;
+  if (!in.get(dense) || !in.get(thr) || !in.get(zeros)) return bad("truncated");
+  const int64_t n = a->ntiles();
+  a->dense = dense != 0;
+  if (!a->dense) {
+    a->norms.resize((size_t)n);
+    if (fread(a->norms.data(), 4, (size_t)n, in.f) != (size_t)n) return bad("truncated");
+    a->threshold = thr;
+    a->zero_count = zeros;
+  }
+  pack_offsets(a.get());
+  tagpu_status st = ensure_storage(a.get());
+  if (st) return st;
+  int64_t count = -1, expect = 0;
+  for (int64_t t = 0; t < n; ++t) expect += a->off[t] >= 0;
+  if (!in.get(count) || count != expect) return bad("stored tiles do not match the shape");
+  PinnedStage stage;
+  if (!stage.p) return fail(ctx, TAGPU_ERR_NOMEM, "load: no pinned staging buffer");
+  int64_t idx[8];
+  for (int64_t c = 0; c < count; ++c) {
+    int64_t t = -1;
+    if (!in.get(t) || t < 0 || t >= n || a->off[t] < 0) return bad("bad tile ordinal");
+    a->tile_index(t, idx);
+    for (uint32_t d = 0; d < rank; ++d) {
+      int64_t lo = 0;
+      if (!in.get(lo) || lo != a->hm[d][idx[d]]) return bad("tile range mismatch");
+    }
+    for (uint32_t d = 0; d < rank; ++d) {
+      int64_t hi = 0;
+      if (!in.get(hi) || hi != a->hm[d][idx[d] + 1]) return bad("tile range mismatch");
+    }
+    const size_t bytes = (size_t)a->tile_volume(t) * sizeof(double);
+    for (size_t x = 0; x < bytes; x += kStage) {
+      const size_t m = std::min(kStage, bytes - x);
+      if (fread(stage.p, 1, m, in.f) != m) return bad("truncated tile data");
+      CUDA_TRY(ctx, cudaMemcpyAsync((uint8_t*)(a->data + a->off[t]) + x, stage.p, m,
+                                    cudaMemcpyHostToDevice, ctx->stream));
+      CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+  }
+  *out_a = a.release();
   return TAGPU_OK;
 }
 
