@@ -472,6 +472,84 @@ def contract(c_idx: str, A: Array, a_idx: str, B: Array, b_idx: str, alpha=1.0,
     return C
 
 
+def general_contract(c_idx: str, A: Array, a_idx: str, B: Array, b_idx: str, alpha=1.0,
+                     threshold=FLT_EPSILON, return_pairs=False):
+    """General (fused-index) product as TiledArray evaluates it
+    (ContEngine::init_struct_general; SparseShape::gemm_batched,
+    sparse_shape.h:1707-1885): indices in both arguments and the target are
+    fused, in both arguments only contracted, in one argument and the target
+    free.  Arguments are permuted to (fused, left free, contracted) and
+    (fused, contracted, right free); every fused-tile slab is screened and
+    contracted as gemm does (same k sizes, no fused-size scaling; outer
+    product norms left*right*|alpha| without contracted modes); each fused
+    element of a slab's tiles is its own matrix product."""
+    ai, bi, ci = parse_indices(a_idx), parse_indices(b_idx), parse_indices(c_idx)
+    F = [x for x in ai if x in bi and x in ci]
+    K = [x for x in ai if x in bi and x not in ci]
+    L = [x for x in ai if x not in bi and x in ci]
+    R = [x for x in bi if x not in ai and x in ci]
+    lperm = perm_between(ai, F + L + K)
+    rperm = perm_between(bi, F + K + R)
+    Al, Br = A.permuted(lperm), B.permuted(rperm)
+    ltr, rtr = Al.tr, Br.tr
+    nf, nl, nk = len(F), len(L), len(K)
+    lnt, rnt = ltr.ntiles(), rtr.ntiles()
+    Ht = int(np.prod(lnt[:nf]))
+    Mt = int(np.prod(lnt[nf:nf + nl])) if nl else 1
+    Kt = int(np.prod(lnt[nf + nl:])) if nk else 1
+    Nt = int(np.prod(rnt[nf + nk:])) if len(R) else 1
+    ln = Al.norms.astype(np.float32).reshape(Ht, Mt, Kt)
+    rn = Br.norms.astype(np.float32).reshape(Ht, Kt, Nt)
+    ks = None
+    if nk:
+        ksv = np.concatenate([np.asarray(ltr.tile_sizes(d), np.float32)
+                              for d in range(nf + nl, ltr.rank)])
+        ks = outer_sizes(lnt[nf + nl:], ksv, False)
+    cn = np.zeros((Ht, Mt, Nt), np.float32)
+    zc = 0
+    offs_all, kidx_all, base = [], [], 0
+    for h in range(Ht):
+        c_h, z_h = shape_gemm(ln[h], rn[h], ks, alpha, threshold)
+        cn[h] = c_h
+        zc += z_h
+        o_h, k_h = pairs(c_h, threshold, ln[h], A.threshold, rn[h], B.threshold)
+        offs_all.append(o_h[:-1] + base)
+        kidx_all.append(k_h)
+        base += int(o_h[-1])
+    offs = np.concatenate(offs_all + [np.asarray([base], np.int64)]).astype(np.int64)
+    kidx = np.concatenate(kidx_all).astype(np.int32) if kidx_all else np.zeros(0, np.int32)
+    res_tr = TiledRange([ltr.dims[d] for d in range(nf + nl)] +
+                        [rtr.dims[d] for d in range(nf + nk, rtr.rank)])
+    C = Array(res_tr, cn.reshape(res_tr.ntiles()), threshold)
+    for h in range(Ht):
+        for t in range(Mt * Nt):
+            if cn[h].ravel()[t] < threshold:
+                continue
+            i, j = divmod(t, Nt)
+            o = (h * Mt + i) * Nt + j
+            lo, hi = res_tr.tile_lo_hi(res_tr.tile_index(o))
+            shp = [hi[d] - lo[d] for d in range(res_tr.rank)]
+            he = int(np.prod(shp[:nf]))
+            m = int(np.prod(shp[nf:nf + nl])) if nl else 1
+            n = int(np.prod(shp[nf + nl:])) if len(R) else 1
+            acc = np.zeros((he, m, n))
+            for p in range(int(offs[o]), int(offs[o + 1])):
+                k = int(kidx[p])
+                ta = Al.tiles.get((h * Mt + i) * Kt + k)
+                tb = Br.tiles.get((h * Kt + k) * Nt + j)
+                if ta is None or tb is None:
+                    continue
+                acc += ta.reshape(he, m, -1) @ tb.reshape(he, -1, n)
+            C.tiles[o] = (alpha * acc).reshape(shp)
+    res = F + L + R
+    if res != ci:
+        C = C.permuted(perm_between(res, ci))
+    if return_pairs:
+        return C, dict(Ht=Ht, Mt=Mt, Nt=Nt, Kt=Kt, offsets=offs, kidx=kidx, cnorm=cn,
+                       zero_count=zc)
+    return C
+
+
 def openblas_dgemm():
     """Address of numpy's bundled ILP64 cblas_dgemm, or None."""
     import numpy

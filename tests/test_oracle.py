@@ -121,3 +121,15 @@ def test_oracle_blas_path_matches_loop(oracle):
     C1 = oracle.contract("i,j", A, "i,k", B, "k,j").to_dense()
     C2 = oracle.contract("i,j", A, "i,k", B, "k,j", use_blas=fn).to_dense()
     assert np.max(np.abs(C1 - C2)) <= 1e-13 * np.max(np.abs(C1))
+
+
+@pytest.mark.parametrize("form", __import__("general_forms").FORMS, ids=lambda f: f[0])
+def test_oracle_general_product_matches_einsum(oracle, form):
+    """The oracle's general product equals numpy.einsum on integer data (exact)."""
+    import general_forms as G
+    tag, c, a, b, tra, trb, sparse = form
+    A = oracle_operand(oracle, tra, 3, 0, kind=1, keep=G.keep_mask(tra, 1) if sparse else None)
+    B = oracle_operand(oracle, trb, 3, 1, kind=1, keep=G.keep_mask(trb, 2) if sparse else None)
+    C = oracle.general_contract(c, A, a, B, b)
+    ref = np.einsum(G.einsum_spec(c, a, b), A.to_dense(), B.to_dense())
+    assert np.array_equal(C.to_dense(), ref)

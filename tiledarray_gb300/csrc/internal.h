@@ -103,6 +103,10 @@ struct GemmView {
   double alpha;
   double* C;
   const int64_t* coff;    // Mt*Nt result offsets, -1 zero tile
+  // general products: this view is element `hel` of a fused-mode slab; the
+  // element's matrix inside a tile of extent (fused..., rows, cols) starts
+  // hel * rows * cols elements into the tile (0 for ordinary contractions)
+  int64_t hel;
 };
 // One 64x64 output block of one result tile of one contraction.
 struct WorkItem {

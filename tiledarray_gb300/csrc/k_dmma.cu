@@ -76,8 +76,8 @@ __global__ void __launch_bounds__(128) dmma_gemm_kernel(const GemmView* __restri
         const int64_t ao = v.aoff[i * v.Kt + k], bo = v.boff[(int64_t)k * v.Nt + j];
         if (ao >= 0 && bo >= 0) {
           kk = v.ksz[k];
-          Ap = v.A + ao;
-          Bp = v.B + bo;
+          Ap = v.A + ao + v.hel * (int64_t)m * kk;
+          Bp = v.B + bo + v.hel * (int64_t)kk * n;
           kcur = 0;
           return true;
         }
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(128) dmma_gemm_kernel(const GemmView* __restri
     }
 
     // epilogue: C block rows r0.., cols c0..
-    double* C = v.C + v.coff[t];
+    double* C = v.C + v.coff[t] + v.hel * (int64_t)m * n;
 #pragma unroll
     for (int x = 0; x < 4; ++x) {
       const int gr = r0 + wm + x * 8 + g;

@@ -1234,6 +1234,15 @@ struct Contraction {
   int inner = 0, lorank = 0;
   std::vector<int> lperm, rperm, cperm;
   int64_t Mt = 1, Nt = 1, Kt = 1;
+  // general products: nfused leading fused (Hadamard) modes in the canonical
+  // layouts (fused, left free, contracted) x (fused, contracted, right free)
+  // -> (fused, left free, right free); Ht fused tiles ("slabs") of hsz
+  // elements each; every per-slab array (norms, offsets, pairs) is stored
+  // slab after slab.  Ordinary contractions: nfused 0, Ht 1.
+  int nfused = 0;
+  int64_t Ht = 1;
+  std::vector<int32_t> hsz{1};
+  std::vector<GemmView> gviews;         // general products: one view per fused element
   std::vector<int32_t> msz, nsz, ksz;
   std::vector<float> kfl;               // k_sizes (float) for the shape gemm
   std::vector<float> ln, rn;            // GEMM-order norms
@@ -1297,6 +1306,79 @@ std::vector<int32_t> fused_sizes(const tagpu_array* a, const std::vector<int>& d
   return out;
 }
 
+// General (fused-index) product, ContEngine::init_struct_general and
+// SparseShape::gemm_batched (sparse_shape.h:1707-1885): indices in both
+// arguments and the target are fused, in both arguments only contracted, in
+// one argument and the target free.  Arguments go to the canonical layouts
+// (fused, left free, contracted) and (fused, contracted, right free), the
+// result is (fused, left free, right free), permuted to the target after.
+tagpu_status plan_general(Contraction& c, tagpu_array* A, tagpu_array* B) {
+  tagpu_ctx* ctx = c.ctx;
+  std::vector<std::string> F, L, K, R;
+  for (auto& x : c.ai) {
+    const bool inB = find_idx(c.bi, x) >= 0, inC = find_idx(c.ci, x) >= 0;
+    if (inB && inC) F.push_back(x);
+    else if (inB) K.push_back(x);
+    else if (inC) L.push_back(x);
+    else return fail(ctx, TAGPU_ERR_UNSUPPORTED, "index '%s' is summed over one argument only",
+                     x.c_str());
+  }
+  for (auto& x : c.bi) {
+    const bool inA = find_idx(c.ai, x) >= 0, inC = find_idx(c.ci, x) >= 0;
+    if (!inA && inC) R.push_back(x);
+    else if (!inA) return fail(ctx, TAGPU_ERR_UNSUPPORTED,
+                               "index '%s' is summed over one argument only", x.c_str());
+  }
+  for (auto& x : c.ci)
+    if (find_idx(c.ai, x) < 0 && find_idx(c.bi, x) < 0)
+      return fail(ctx, TAGPU_ERR_INVALID, "target index '%s' is in neither argument", x.c_str());
+  if (c.ci.size() != F.size() + L.size() + R.size())
+    return fail(ctx, TAGPU_ERR_INVALID, "target indices repeat");
+  c.po = PermOpt{};
+  c.po.left = F;
+  c.po.left.insert(c.po.left.end(), L.begin(), L.end());
+  c.po.left.insert(c.po.left.end(), K.begin(), K.end());
+  c.po.right = F;
+  c.po.right.insert(c.po.right.end(), K.begin(), K.end());
+  c.po.right.insert(c.po.right.end(), R.begin(), R.end());
+  c.po.result = F;
+  c.po.result.insert(c.po.result.end(), L.begin(), L.end());
+  c.po.result.insert(c.po.result.end(), R.begin(), R.end());
+  c.po.lop = c.po.rop = GENERAL;
+  c.nfused = (int)F.size();
+  c.inner = (int)K.size();
+  c.lorank = (int)L.size();
+  c.lperm = perm_between(c.ai, c.po.left);
+  c.rperm = perm_between(c.bi, c.po.right);
+  c.cperm = perm_between(c.po.result, c.ci);
+  std::vector<int> f_dims, lo_dims, li_dims, ro_dims;
+  for (auto& x : F) f_dims.push_back(find_idx(c.ai, x));
+  for (auto& x : L) lo_dims.push_back(find_idx(c.ai, x));
+  for (auto& x : K) li_dims.push_back(find_idx(c.ai, x));
+  for (auto& x : R) ro_dims.push_back(find_idx(c.bi, x));
+  for (auto* v : {&F, &K})
+    for (auto& x : *v)
+      if (A->hm[find_idx(c.ai, x)] != B->hm[find_idx(c.bi, x)])
+        return fail(ctx, TAGPU_ERR_INVALID,
+                    "the %s dimensions '%s' of the arguments are not congruent",
+                    v == &F ? "fused" : "contracted", x.c_str());
+  c.hsz = fused_sizes(A, f_dims);
+  c.Ht = (int64_t)c.hsz.size();
+  c.msz = fused_sizes(A, lo_dims);
+  c.ksz = fused_sizes(A, li_dims);
+  c.nsz = fused_sizes(B, ro_dims);
+  c.Mt = (int64_t)c.msz.size();
+  c.Kt = (int64_t)c.ksz.size();
+  c.Nt = (int64_t)c.nsz.size();
+  if (c.inner > 0) {
+    auto sv = size_vectors(A);
+    std::vector<std::vector<float>> ksv;
+    for (int d : li_dims) ksv.push_back(sv[d]);
+    c.kfl = outer_sizes(ksv, 0, ksv.size(), false);
+  }
+  return TAGPU_OK;
+}
+
 // Parse, classify, choose layouts, GEMM-order sizes and norms.
 tagpu_status plan_contraction(Contraction& c, const char* c_idx, double alpha, tagpu_array* A,
                               const char* a_idx, tagpu_array* B, const char* b_idx,
@@ -1308,6 +1390,27 @@ tagpu_status plan_contraction(Contraction& c, const char* c_idx, double alpha, t
     return fail(ctx, TAGPU_ERR_INVALID, "index list rank does not match the array rank");
   if (A->dense != B->dense)
     return fail(ctx, TAGPU_ERR_UNSUPPORTED, "dense and sparse arguments cannot be mixed");
+  bool general = false;
+  for (auto& x : c.ci)
+    general = general || (find_idx(c.ai, x) >= 0 && find_idx(c.bi, x) >= 0);
+  if (general) {
+    tagpu_status e = plan_general(c, A, B);
+    if (e) return e;
+    c.dense = A->dense;
+    c.alpha = alpha;
+    c.cthr = cthr;
+    if (c.dense) {
+      c.ln.assign(c.Ht * c.Mt * c.Kt, 1.0f);
+      c.rn.assign(c.Ht * c.Kt * c.Nt, 1.0f);
+      c.lthr = c.rthr = 0.0f;
+    } else {
+      c.ln = permute_grid(A->norms, A->nt, c.lperm);
+      c.rn = permute_grid(B->norms, B->nt, c.rperm);
+      c.lthr = A->threshold;
+      c.rthr = B->threshold;
+    }
+    return TAGPU_OK;
+  }
   // TensorProduct::Contraction: every target index is free in exactly one
   // argument, every other index is shared by both arguments
   for (auto& x : c.ci) {
@@ -1372,70 +1475,83 @@ tagpu_status plan_contraction(Contraction& c, const char* c_idx, double alpha, t
   return TAGPU_OK;
 }
 
-// Steps (a) and (b) on the device.
+// Steps (a) and (b) on the device, slab by slab for general products
+// (SparseShape::gemm_batched contracts every fused-tile slab as gemm does).
 tagpu_status run_shape_and_pairs(Contraction& c) {
   tagpu_ctx* ctx = c.ctx;
   cudaStream_t s = ctx->stream;
-  const int64_t MN = c.Mt * c.Nt;
+  const int64_t H = c.Ht, MN = c.Mt * c.Nt, TOT = H * MN;
+  const int64_t lslab = c.Mt * c.Kt, rslab = c.Kt * c.Nt;   // per-slab norm counts
   DBuf dL(ctx), dR(ctx), dK(ctx), dC(ctx), dz(ctx), dcnt(ctx), dfl(ctx);
   tagpu_status e;
   if ((e = upload_vec(ctx, dL, c.ln)) || (e = upload_vec(ctx, dR, c.rn)) ||
       (e = upload_vec(ctx, dK, c.kfl)) || (e = upload_vec(ctx, c.d_msz, c.msz)) ||
       (e = upload_vec(ctx, c.d_nsz, c.nsz)) || (e = upload_vec(ctx, c.d_ksz, c.ksz)))
     return e;
-  if ((e = dC.alloc(std::max<int64_t>(1, MN) * sizeof(float))) ||
+  if ((e = dC.alloc(std::max<int64_t>(1, TOT) * sizeof(float))) ||
       (e = dz.alloc(sizeof(unsigned long long))) ||
-      (e = dcnt.alloc(std::max<int64_t>(1, MN) * sizeof(int64_t))) ||
-      (e = dfl.alloc(sizeof(double))) || (e = c.d_poff.alloc((MN + 1) * sizeof(int64_t))))
+      (e = dcnt.alloc(std::max<int64_t>(1, TOT) * sizeof(int64_t))) ||
+      (e = dfl.alloc(std::max<int64_t>(1, H) * sizeof(double))) ||
+      (e = c.d_poff.alloc((TOT + 1) * sizeof(int64_t))))
     return e;
   CUDA_TRY(ctx, cudaMemsetAsync(dz.p, 0, sizeof(unsigned long long), s));
-  CUDA_TRY(ctx, cudaMemsetAsync(dfl.p, 0, sizeof(double), s));
+  CUDA_TRY(ctx, cudaMemsetAsync(dfl.p, 0, std::max<int64_t>(1, H) * sizeof(double), s));
   const float af = (float)std::fabs(c.alpha);
   {
     EventTimer tm(s);
     if (c.dense) {
       // DenseShape::gemm (dense_shape.h:378-390): every result tile present
-      std::vector<float> ones(std::max<int64_t>(1, MN), 1.0f);
+      std::vector<float> ones(std::max<int64_t>(1, TOT), 1.0f);
       CUDA_TRY(ctx, cudaMemcpyAsync(dC.p, ones.data(), ones.size() * sizeof(float),
                                     cudaMemcpyHostToDevice, s));
       CUDA_TRY(ctx, cudaStreamSynchronize(s));
     } else if (c.inner > 0 && c.kfl.empty()) {
-      CUDA_TRY(ctx, cudaMemsetAsync(dC.p, 0, std::max<int64_t>(1, MN) * sizeof(float), s));
-      unsigned long long z = 0.0f < c.cthr ? (unsigned long long)MN : 0ull;
+      CUDA_TRY(ctx, cudaMemsetAsync(dC.p, 0, std::max<int64_t>(1, TOT) * sizeof(float), s));
+      unsigned long long z = 0.0f < c.cthr ? (unsigned long long)TOT : 0ull;
       CUDA_TRY(ctx, cudaMemcpyAsync(dz.p, &z, sizeof(z), cudaMemcpyHostToDevice, s));
       CUDA_TRY(ctx, cudaStreamSynchronize(s));
     } else {
-      launch_shape_gemm(s, c.Mt, c.Nt, c.inner > 0 ? c.Kt : 0, dL.as<float>(), dR.as<float>(),
-                        dK.as<float>(), af, c.cthr, dC.as<float>(),
-                        dz.as<unsigned long long>());
+      for (int64_t h = 0; h < H; ++h)
+        launch_shape_gemm(s, c.Mt, c.Nt, c.inner > 0 ? c.Kt : 0, dL.as<float>() + h * lslab,
+                          dR.as<float>() + h * rslab, dK.as<float>(), af, c.cthr,
+                          dC.as<float>() + h * MN, dz.as<unsigned long long>());
     }
     tm.stop();
     CUDA_TRY(ctx, cudaGetLastError());
     c.st.ms_shape = tm.ms();
   }
-  c.cn.resize(MN);
+  c.cn.resize(TOT);
   unsigned long long zc = 0;
-  if (MN)
-    CUDA_TRY(ctx, cudaMemcpyAsync(c.cn.data(), dC.p, MN * sizeof(float), cudaMemcpyDeviceToHost,
+  if (TOT)
+    CUDA_TRY(ctx, cudaMemcpyAsync(c.cn.data(), dC.p, TOT * sizeof(float), cudaMemcpyDeviceToHost,
                                   s));
   CUDA_TRY(ctx, cudaMemcpyAsync(&zc, dz.p, sizeof(zc), cudaMemcpyDeviceToHost, s));
   {
     EventTimer tm(s);
     const float cthr = c.dense ? 0.0f : c.cthr;
-    launch_pair_count(s, c.Mt, c.Nt, c.Kt, dC.as<float>(), cthr, dL.as<float>(), c.lthr,
-                      dR.as<float>(), c.rthr, c.d_msz.as<int32_t>(), c.d_nsz.as<int32_t>(),
-                      c.d_ksz.as<int32_t>(), dcnt.as<int64_t>(), dfl.as<double>());
-    launch_exclusive_scan(s, dcnt.as<int64_t>(), MN, c.d_poff.as<int64_t>());
+    for (int64_t h = 0; h < H; ++h)
+      launch_pair_count(s, c.Mt, c.Nt, c.Kt, dC.as<float>() + h * MN, cthr,
+                        dL.as<float>() + h * lslab, c.lthr, dR.as<float>() + h * rslab, c.rthr,
+                        c.d_msz.as<int32_t>(), c.d_nsz.as<int32_t>(), c.d_ksz.as<int32_t>(),
+                        dcnt.as<int64_t>() + h * MN, dfl.as<double>() + h);
+    launch_exclusive_scan(s, dcnt.as<int64_t>(), TOT, c.d_poff.as<int64_t>());
     CUDA_TRY(ctx, cudaGetLastError());
     int64_t np = 0;
-    CUDA_TRY(ctx, cudaMemcpyAsync(&np, c.d_poff.as<int64_t>() + MN, sizeof(int64_t),
+    std::vector<double> fl(std::max<int64_t>(1, H), 0.0);
+    CUDA_TRY(ctx, cudaMemcpyAsync(&np, c.d_poff.as<int64_t>() + TOT, sizeof(int64_t),
                                   cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(ctx, cudaMemcpyAsync(&c.flops, dfl.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(ctx, cudaMemcpyAsync(fl.data(), dfl.p, fl.size() * sizeof(double),
+                                  cudaMemcpyDeviceToHost, s));
     CUDA_TRY(ctx, cudaStreamSynchronize(s));
     c.npairs = np;
+    // a slab's tile pairs run once per fused element of the slab
+    c.flops = 0.0;
+    for (int64_t h = 0; h < H; ++h) c.flops += fl[h] * (double)c.hsz[h];
     if ((e = c.d_kidx.alloc(std::max<int64_t>(1, np) * sizeof(int32_t)))) return e;
-    launch_pair_emit(s, c.Mt, c.Nt, c.Kt, dC.as<float>(), cthr, dL.as<float>(), c.lthr,
-                     dR.as<float>(), c.rthr, c.d_poff.as<int64_t>(), c.d_kidx.as<int32_t>());
+    for (int64_t h = 0; h < H; ++h)
+      launch_pair_emit(s, c.Mt, c.Nt, c.Kt, dC.as<float>() + h * MN, cthr,
+                       dL.as<float>() + h * lslab, c.lthr, dR.as<float>() + h * rslab, c.rthr,
+                       c.d_poff.as<int64_t>() + h * MN, c.d_kidx.as<int32_t>());
     tm.stop();
     CUDA_TRY(ctx, cudaGetLastError());
     c.st.ms_pairs = tm.ms();
@@ -1479,9 +1595,13 @@ tagpu_status prepare_operands(Contraction& c, tagpu_array* A, tagpu_array* B) {
     c.Bop = B;
     c.b_trans = (c.po.rop == MATRIX_TRANSPOSE && !is_identity(c.rperm)) ? 1 : 0;
   }
-  c.aoff.assign(c.Mt * c.Kt, -1);
-  c.boff.assign(c.Kt * c.Nt, -1);
-  if (c.inner == 0) {
+  c.aoff.assign(c.Ht * c.Mt * c.Kt, -1);
+  c.boff.assign(c.Ht * c.Kt * c.Nt, -1);
+  if (c.nfused > 0) {
+    // canonical layouts: the argument's own tile order, slab after slab
+    for (int64_t t = 0; t < (int64_t)c.aoff.size(); ++t) c.aoff[t] = c.Aop->off[t];
+    for (int64_t t = 0; t < (int64_t)c.boff.size(); ++t) c.boff[t] = c.Bop->off[t];
+  } else if (c.inner == 0) {
     for (int64_t m = 0; m < c.Mt; ++m) c.aoff[m] = c.Aop->off[m];
     for (int64_t n = 0; n < c.Nt; ++n) c.boff[n] = c.Bop->off[n];
     c.a_trans = c.b_trans = 0;
@@ -1503,8 +1623,10 @@ tagpu_status prepare_operands(Contraction& c, tagpu_array* A, tagpu_array* B) {
 tagpu_status make_result(Contraction& c, tagpu_array* A, tagpu_array* B) {
   tagpu_ctx* ctx = c.ctx;
   std::vector<std::vector<int64_t>> hm;
-  for (int x = 0; x < c.lorank; ++x) hm.push_back(A->hm[find_idx(c.ai, c.po.left[x])]);
-  for (size_t x = c.inner; x < c.po.right.size(); ++x)
+  // fused modes (general products), then the left outer, then the right outer
+  for (int x = 0; x < c.nfused + c.lorank; ++x)
+    hm.push_back(A->hm[find_idx(c.ai, c.po.left[x])]);
+  for (size_t x = c.nfused + c.inner; x < c.po.right.size(); ++x)
     hm.push_back(B->hm[find_idx(c.bi, c.po.right[x])]);
   c.C.reset(new_array(ctx, hm));
   tagpu_array* C = c.C.get();
@@ -1518,7 +1640,7 @@ tagpu_status make_result(Contraction& c, tagpu_array* A, tagpu_array* B) {
   pack_offsets(C);
   tagpu_status e = ensure_storage(C);
   if (e) return e;
-  std::vector<int64_t> coff(c.Mt * c.Nt, -1);
+  std::vector<int64_t> coff(c.Ht * c.Mt * c.Nt, -1);
   for (int64_t t = 0; t < (int64_t)coff.size() && t < C->ntiles(); ++t) coff[t] = C->off[t];
   if ((e = upload_vec(ctx, c.d_coff, coff))) return e;
   if (!is_identity(c.cperm)) {
@@ -1568,6 +1690,39 @@ tagpu_status build_dmma_items(Contraction& c, int32_t view) {
 }
 
 // Full planning of one contraction.
+// General products: one view per fused element (the slab's tile, pair and
+// result offsets; the element's matrices inside the slab's tiles) and the
+// work items of its nonzero result tiles.
+tagpu_status build_general_items(Contraction& c) {
+  c.items.clear();
+  c.gviews.clear();
+  const GemmView base = gemm_view(c);
+  const int64_t MN = c.Mt * c.Nt;
+  for (int64_t h = 0; h < c.Ht; ++h) {
+    for (int64_t el = 0; el < c.hsz[h]; ++el) {
+      GemmView v = base;
+      v.aoff = base.aoff + h * c.Mt * c.Kt;
+      v.boff = base.boff + h * c.Kt * c.Nt;
+      v.poff = base.poff + h * MN;
+      v.coff = base.coff + h * MN;
+      v.hel = el;
+      const int32_t vid = (int32_t)c.gviews.size();
+      c.gviews.push_back(v);
+      for (int64_t t = 0; t < MN; ++t) {
+        if (c.C->off[h * MN + t] < 0) continue;
+        const int64_t i = t / c.Nt, j = t % c.Nt;
+        const int64_t rbs = (c.msz[i] + 63) / 64, cbs = (c.nsz[j] + 63) / 64;
+        if (rbs > 32767 || cbs > 32767)
+          return fail(c.ctx, TAGPU_ERR_UNSUPPORTED, "fused tile extent above 2097088");
+        for (int64_t rb = 0; rb < rbs; ++rb)
+          for (int64_t cb = 0; cb < cbs; ++cb)
+            c.items.push_back(WorkItem{t, vid, (int16_t)rb, (int16_t)cb});
+      }
+    }
+  }
+  return TAGPU_OK;
+}
+
 tagpu_status plan_all(Contraction& c, const char* c_idx, double alpha, tagpu_array* A,
                       const char* a_idx, tagpu_array* B, const char* b_idx,
                       const tagpu_contract_opts* opts) {
@@ -1582,11 +1737,16 @@ tagpu_status plan_all(Contraction& c, const char* c_idx, double alpha, tagpu_arr
   tagpu_status e;
   std::string err;
   if ((e = plan_contraction(c, c_idx, alpha, A, a_idx, B, b_idx, cthr))) return e;
+  if (c.nfused > 0 && c.precision == TAGPU_PRECISION_OZAKI)
+    return fail(ctx, TAGPU_ERR_UNSUPPORTED,
+                "general (fused-index) products run in the plain FP64 form only");
   if ((e = run_shape_and_pairs(c))) return e;
   if ((e = make_result(c, A, B))) return e;
   if ((e = prepare_operands(c, A, B))) return e;
   c.view = gemm_view(c);
-  if (c.precision == TAGPU_PRECISION_OZAKI && c.npairs > 0 && c.C->elements > 0) {
+  if (c.nfused > 0) {
+    if ((e = build_general_items(c))) return e;
+  } else if (c.precision == TAGPU_PRECISION_OZAKI && c.npairs > 0 && c.C->elements > 0) {
     e = ozaki_plan(ctx->stream, c.view, c.msz.data(), c.nsz.data(), c.ksz.data(), c.slices,
                    &c.oz, &err);
     if (e) return fail(ctx, e, "%s", err.c_str());
@@ -1616,7 +1776,7 @@ tagpu_status plan_all(Contraction& c, const char* c_idx, double alpha, tagpu_arr
 
 void fill_stats(Contraction& c) {
   tagpu_contract_stats& st = c.st;
-  st.result_tiles = c.Mt * c.Nt;
+  st.result_tiles = c.Ht * c.Mt * c.Nt;
   int64_t nz = 0;
   for (auto o : c.result()->off) nz += o >= 0;
   st.nonzero_result_tiles = nz;
@@ -1690,10 +1850,13 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, Launch
   for (auto* c : cs) {
     if (c->view.C == nullptr || c->emulated()) continue;
     {
-      const int32_t vid = (int32_t)views.size();
-      views.push_back(c->view);
+      const int32_t base = (int32_t)views.size();
+      if (c->gviews.empty())
+        views.push_back(c->view);
+      else
+        views.insert(views.end(), c->gviews.begin(), c->gviews.end());
       for (WorkItem w : c->items) {
-        w.view = vid;
+        w.view += base;
         items.push_back(w);
       }
     }
