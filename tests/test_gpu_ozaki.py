@@ -95,6 +95,23 @@ def test_ozaki_long_k_exact(ta, world):
     assert np.array_equal(C.download(), Cp.download())
 
 
+@pytest.mark.parametrize("c,a,b", [("i,j", "i,k", "k,j"), ("i,j", "k,i", "j,k")])
+def test_ozaki_tiny_tiles_exact(ta, world, c, a, b):
+    """One-element tiles along rows and k: a 128 x 32 brick overlaps 4096
+    tiles, more than the split stages, so tile offsets are looked up per
+    element; both storage orders of A and B."""
+    ones = list(range(0, 161))
+    hn = [0, 50, 97]
+    tra = [ones, ones]
+    trb = [ones, hn] if b == "k,j" else [hn, ones]
+    keep_a = (np.arange(160 * 160).reshape(160, 160) % 7 != 3).astype(float)
+    A, _ = gpu_operand(ta, world, tra, 3, 0, kind=1, keep=keep_a)
+    B, _ = gpu_operand(ta, world, trb, 3, 1, kind=1)
+    C, _ = ta.contract(world, c, 1.0, A, a, B, b, precision=ta.PRECISION_OZAKI)
+    Cp, _ = ta.contract(world, c, 1.0, A, a, B, b)
+    assert np.array_equal(C.to_dense(C.trange), Cp.to_dense(Cp.trange))
+
+
 def test_ozaki_transposed_and_4index(oracle, ta, world):
     h1, h2 = [0, 40, 96], [0, 32, 70, 96]
     for c, a, b, tra, trb in [("i,j", "k,i", "j,k", [h2, h1], [h1, h2]),

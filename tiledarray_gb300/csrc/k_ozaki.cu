@@ -782,11 +782,11 @@ __global__ void zero_kernel(const ZeroJob* __restrict__ jobs) {
   for (int64_t i = threadIdx.x; i < J.n; i += blockDim.x) J.p[i] = 0;
 }
 
-// Digits of one element into the brick image in shared memory:
-// fixed point round(x * 2^(8S-1-E)) (E = frame - 1022), cut into S balanced
-// base-256 digits, least significant first, each stored as exact bf16.
-template <int S, int SLICE>
-__device__ __forceinline__ void split_store(double x, int frame, int r, int k, uint8_t* img) {
+// Digits of one element: fixed point round(x * 2^(8S-1-E)) (E = frame -
+// 1022), cut into S balanced base-256 digits, least significant first, each
+// returned as the bit pattern of the exact bf16 (|d| <= 128).
+template <int S>
+__device__ __forceinline__ void split_digits(double x, int frame, uint32_t (&h)[S]) {
   int64_t fx = 0;
   const uint64_t bits = (uint64_t)__double_as_longlong(x);
   const int be = (int)((bits >> 52) & 0x7ff);
@@ -810,19 +810,13 @@ __device__ __forceinline__ void split_store(double x, int frame, int r, int k, u
     }
     fx = (bits >> 63) ? -(int64_t)q : (int64_t)q;
   }
-  int dig[S];
 #pragma unroll
   for (int p = S - 1; p >= 1; --p) {
     const int d = (int)(((fx + 128) & 255) - 128);
-    dig[p] = d;
+    h[p] = __float_as_uint((float)d) >> 16;
     fx = (fx - d) >> 8;
   }
-  dig[0] = (int)fx;
-  const uint32_t bo = brick_offset(r, k);
-#pragma unroll
-  for (int p = 0; p < S; ++p)
-    *reinterpret_cast<uint16_t*>(img + p * SLICE + bo) =
-        (uint16_t)(__float_as_uint((float)dig[p]) >> 16);  // exact: |d| <= 128
+  h[0] = __float_as_uint((float)fx) >> 16;
 }
 
 // A split job: the bricks of one operand (or of one row chunk of it) of one
@@ -839,41 +833,61 @@ struct SplitJob {
   int64_t brick0;
 };
 
+// Split staging layout in shared memory: the 16 bytes of (row r, k group
+// g = k / 8) sit at chunk g * (ROWS + 1) + r of a slice.  The four k groups
+// of one row land in distinct bank groups (lanes along k store 2 bytes each
+// without conflicts) and the rows of one group are consecutive chunks (lanes
+// along rows store 16 bytes each without conflicts).  The copy-out reorders
+// the chunks into the K-major core-matrix image (brick_offset).
+template <int ROWS>
+__device__ __forceinline__ uint32_t stage_chunk(int r, int g) {
+  return (uint32_t)(g * (ROWS + 1) + r) * 16;
+}
+
 // One CTA per brick (grid-stride over the bricks of all jobs): gather
 // ROWS x 32 elements, split them into S digit slices, write the brick image.
-// The brick's row and k maps (tile, local index, frame, tile extent) are
-// staged in shared memory first, so an element costs one tile-offset lookup
-// and one data load.  Row-major tiles are read by warps along rows with
-// lanes along k, transposed tiles with lanes along rows: both coalesced.
+// The brick's row and k maps (tile, local index, frame, tile extent) and the
+// offsets of the tiles it overlaps are staged in shared memory first, so an
+// element costs one independent data load; a thread issues all its loads
+// before it splits.  Row-major tiles are read by warps along rows with lanes
+// along k, transposed tiles by threads that own eight k of one row with
+// lanes along rows: both coalesced.  A brick over more than kTable tiles
+// (tiles of a few elements) looks tile offsets up in global memory.
 template <int S, int ROWS>
-__global__ void __launch_bounds__(256) split_kernel(const SplitJob* __restrict__ jobs, int njobs,
+__global__ void __launch_bounds__(256, ROWS == BM ? 3 : 5) split_kernel(const SplitJob* __restrict__ jobs, int njobs,
                                                     int64_t total) {
-  constexpr int SLICE = ROWS * BK * 2;
+  constexpr int SLICE = ROWS * BK * 2;        // image bytes per slice
+  constexpr int SPAD = 4 * (ROWS + 1) * 16;   // staged bytes per slice
+  constexpr int EPT = ROWS * BK / 256;        // elements per thread
+  constexpr int kTable = 256;
+  static_assert(EPT % 8 == 0, "a transposed-tile thread owns whole k groups");
   extern __shared__ __align__(16) uint8_t img[];
   __shared__ int s_rt[ROWS], s_lr[ROWS], s_fr[ROWS], s_m[ROWS];
   __shared__ int s_kt[BK], s_lk[BK], s_kk[BK];
+  __shared__ int64_t s_off[kTable];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nwarps = blockDim.x >> 5;
   for (int64_t gbi = blockIdx.x; gbi < total; gbi += gridDim.x) {
     int lo = 0, hi = njobs;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
       if (jobs[mid].brick0 <= gbi) lo = mid; else hi = mid;
     }
-    const SplitJob J = jobs[lo];
+    const SplitJob& J = jobs[lo];
     const OperandView& v = J.v;
-    const int32_t *row_tile = J.row_tile, *row_local = J.row_local;
-    const int32_t *k_tile = J.k_tile, *k_local = J.k_local, *E = J.E;
     const int64_t rows_total = J.rows_total, k_total = J.k_total;
     const int64_t bi = gbi - J.brick0;
-    const int rbk = J.bricks[2 * bi], kbk = J.bricks[2 * bi + 1];
+    const int64_t r0 = (int64_t)J.bricks[2 * bi] * ROWS, k0 = (int64_t)J.bricks[2 * bi + 1] * BK;
+    const int rt0 = J.row_tile[r0], kt0 = J.k_tile[k0];
+    const int nr = J.row_tile[min(rows_total, r0 + ROWS) - 1] - rt0 + 1;
+    const int nk = J.k_tile[min(k_total, k0 + BK) - 1] - kt0 + 1;
+    const bool staged = nr * nk <= kTable;
     for (int i = threadIdx.x; i < ROWS; i += blockDim.x) {
-      const int64_t gr = (int64_t)rbk * ROWS + i;
+      const int64_t gr = r0 + i;
       if (gr < rows_total) {
-        const int rt = row_tile[gr];
+        const int rt = J.row_tile[gr];
         s_rt[i] = rt;
-        s_lr[i] = row_local[gr];
-        s_fr[i] = E[gr];
+        s_lr[i] = J.row_local[gr];
+        s_fr[i] = J.E[gr];
         s_m[i] = v.rsz[rt];
       } else {
         s_rt[i] = -1;
@@ -881,49 +895,103 @@ __global__ void __launch_bounds__(256) split_kernel(const SplitJob* __restrict__
       }
     }
     if (threadIdx.x < BK) {
-      const int64_t gk = (int64_t)kbk * BK + threadIdx.x;
+      const int64_t gk = k0 + threadIdx.x;
       if (gk < k_total) {
-        const int kt = k_tile[gk];
+        const int kt = J.k_tile[gk];
         s_kt[threadIdx.x] = kt;
-        s_lk[threadIdx.x] = k_local[gk];
+        s_lk[threadIdx.x] = J.k_local[gk];
         s_kk[threadIdx.x] = v.ksz[kt];
       } else {
         s_kt[threadIdx.x] = -1;
       }
     }
-    __syncthreads();
-    if (!v.row_contig) {
-      // element (r, k) at o + lr * kk + lk: lanes along k
-      const int k = lane, kt = s_kt[k], lk = s_lk[k], kk = kt >= 0 ? s_kk[k] : 0;
-#pragma unroll 4
-      for (int r = warp; r < ROWS; r += nwarps) {
-        const int rt = s_rt[r];
-        double x = 0.0;
-        if (rt >= 0 && kt >= 0) {
-          const int64_t o = v.off[(int64_t)rt * v.off_stride_row + (int64_t)kt * v.off_stride_k];
-          if (o >= 0) x = v.data[o + (int64_t)s_lr[r] * kk + lk];
-        }
-        split_store<S, SLICE>(x, s_fr[r], r, k, img);
-      }
-    } else {
-      // element (r, k) at o + lk * m + lr: lanes along rows
-#pragma unroll 4
-      for (int it = warp; it < BK * (ROWS / 32); it += nwarps) {
-        const int k = it % BK, r = (it / BK) * 32 + lane;
-        const int rt = s_rt[r], kt = s_kt[k];
-        double x = 0.0;
-        if (rt >= 0 && kt >= 0) {
-          const int64_t o = v.off[(int64_t)rt * v.off_stride_row + (int64_t)kt * v.off_stride_k];
-          if (o >= 0) x = v.data[o + (int64_t)s_lk[k] * s_m[r] + s_lr[r]];
-        }
-        split_store<S, SLICE>(x, s_fr[r], r, k, img);
+    if (staged) {
+      for (int t = threadIdx.x; t < nr * nk; t += blockDim.x) {
+        const int a = t / nk, b = t - a * nk;
+        s_off[t] = v.off[(int64_t)(rt0 + a) * v.off_stride_row + (int64_t)(kt0 + b) * v.off_stride_k];
       }
     }
     __syncthreads();
-    uint4* dst = reinterpret_cast<uint4*>(J.pack + (size_t)bi * S * SLICE);
-    const uint4* src = reinterpret_cast<const uint4*>(img);
-    for (int i = threadIdx.x; i < S * SLICE / 16; i += blockDim.x) dst[i] = src[i];
+    const double* __restrict__ data = v.data;
+    auto tile_off = [&](int rt, int kt) -> int64_t {
+      return staged ? s_off[(rt - rt0) * nk + (kt - kt0)]
+                    : v.off[(int64_t)rt * v.off_stride_row + (int64_t)kt * v.off_stride_k];
+    };
+    double x[EPT];
+    if (!v.row_contig) {
+      // element (r, k) at o + lr * kk + lk: lanes along k, rows warp + 8 i
+      const int k = lane, kt = s_kt[k], lk = s_lk[k], kk = kt >= 0 ? s_kk[k] : 0;
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        const int r = warp + 8 * i, rt = s_rt[r];
+        double val = 0.0;
+        if (rt >= 0 && kt >= 0) {
+          const int64_t o = tile_off(rt, kt);
+          if (o >= 0) val = data[o + (int64_t)s_lr[r] * kk + lk];
+        }
+        x[i] = val;
+      }
+      uint8_t* c0 = img + stage_chunk<ROWS>(0, k >> 3) + (k & 7) * 2;
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        const int r = warp + 8 * i;
+        uint32_t h[S];
+        split_digits<S>(x[i], s_fr[r], h);
+#pragma unroll
+        for (int p = 0; p < S; ++p)
+          *reinterpret_cast<uint16_t*>(c0 + r * 16 + p * SPAD) = (uint16_t)h[p];
+      }
+    } else {
+      // element (r, k) at o + lk * m + lr: a thread owns row r = 32 (item / 4)
+      // + lane and the eight k of group item % 4
+#pragma unroll
+      for (int i = 0; i < EPT / 8; ++i) {
+        const int item = warp + 8 * i, r = (item >> 2) * 32 + lane, g = item & 3;
+        const int rt = s_rt[r], lr = s_lr[r], m = s_m[r];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int k = 8 * g + j, kt = s_kt[k];
+          double val = 0.0;
+          if (rt >= 0 && kt >= 0) {
+            const int64_t o = tile_off(rt, kt);
+            if (o >= 0) val = data[o + (int64_t)s_lk[k] * m + lr];
+          }
+          x[8 * i + j] = val;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < EPT / 8; ++i) {
+        const int item = warp + 8 * i, r = (item >> 2) * 32 + lane, g = item & 3;
+        const int fr = s_fr[r];
+        uint32_t w[S][4];
+#pragma unroll
+        for (int p = 0; p < S; ++p) w[p][0] = w[p][1] = w[p][2] = w[p][3] = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          uint32_t h[S];
+          split_digits<S>(x[8 * i + j], fr, h);
+#pragma unroll
+          for (int p = 0; p < S; ++p) w[p][j >> 1] |= h[p] << (16 * (j & 1));
+        }
+        uint8_t* c = img + stage_chunk<ROWS>(r, g);
+#pragma unroll
+        for (int p = 0; p < S; ++p)
+          *reinterpret_cast<uint4*>(c + p * SPAD) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+      }
+    }
     __syncthreads();
+    // Copy-out in image order (chunk c of a slice: row 8 (c / 32) + c % 8,
+    // k group (c / 8) % 4).  The maps and staged offsets are not read again,
+    // so the next brick may restage them while slow threads still copy; its
+    // first barrier orders its stores into img after this copy.
+    constexpr int CH = SLICE / 16;
+    uint8_t* dst = J.pack + (size_t)bi * S * SLICE;
+    for (int i = threadIdx.x; i < S * CH; i += blockDim.x) {
+      const int p = i / CH, c = i - p * CH;
+      const int r = (c >> 5) * 8 + (c & 7), g = (c >> 3) & 3;   // brick_offset(r, 8 g) == 16 c
+      *reinterpret_cast<uint4*>(dst + p * SLICE + brick_offset(r, 8 * g)) =
+          *reinterpret_cast<const uint4*>(img + p * SPAD + stage_chunk<ROWS>(r, g));
+    }
   }
 }
 
@@ -1174,26 +1242,37 @@ void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int
   }
 }
 
+// Dynamic shared memory of a split CTA: S staged slices of ROWS x 32 digits.
+constexpr int split_smem(int S, int rows) { return S * 4 * (rows + 1) * 16; }
+
 template <int S>
 void launch_split_t(const SplitJob* d_jobs, int njobs, int64_t total, bool a_side,
                     int sm_count, cudaStream_t st) {
-  // the shared-memory attribute is per device
+  // the shared-memory attribute and the residency are per device
   static bool set[kMaxDevices] = {};
+  static int resident[kMaxDevices][2] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < kMaxDevices && !set[dev]) {
+  if (dev < 0 || dev >= kMaxDevices) dev = 0;
+  if (!set[dev]) {
     cudaFuncSetAttribute(split_kernel<S, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         S * A_SLICE_BYTES);
+                         split_smem(S, BM));
     cudaFuncSetAttribute(split_kernel<S, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         S * B_SLICE_BYTES);
+                         split_smem(S, BN));
+    int ra = 0, rb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ra, split_kernel<S, BM>, 256, split_smem(S, BM));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rb, split_kernel<S, BN>, 256, split_smem(S, BN));
+    resident[dev][0] = std::max(ra, 1);
+    resident[dev][1] = std::max(rb, 1);
     set[dev] = true;
   }
   if (total <= 0 || njobs <= 0) return;
-  const int grid = (int)std::min<int64_t>(total, (int64_t)sm_count * 8);
+  // one wave of resident CTAs, each striding over the bricks
+  const int grid = (int)std::min<int64_t>(total, (int64_t)sm_count * resident[dev][a_side ? 0 : 1]);
   if (a_side)
-    split_kernel<S, BM><<<grid, 256, S * A_SLICE_BYTES, st>>>(d_jobs, njobs, total);
+    split_kernel<S, BM><<<grid, 256, split_smem(S, BM), st>>>(d_jobs, njobs, total);
   else
-    split_kernel<S, BN><<<grid, 256, S * B_SLICE_BYTES, st>>>(d_jobs, njobs, total);
+    split_kernel<S, BN><<<grid, 256, split_smem(S, BN), st>>>(d_jobs, njobs, total);
   count_launch();
 }
 
