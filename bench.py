@@ -123,6 +123,55 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def host_placement(arrays, device=0):
+    """Where the e2e host buffers live: pages per NUMA node of each buffer
+    (from /proc/self/numa_maps), the NUMA node of the GPU's PCI function,
+    and the CPUs and memory nodes this process may use."""
+    info = {"cpus": len(os.sched_getaffinity(0))}
+    try:
+        for line in open("/proc/self/status"):
+            if line.startswith("Mems_allowed_list:"):
+                info["mems_allowed"] = line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    try:
+        import torch
+        pr = torch.cuda.get_device_properties(device)
+        bus = "%04x:%02x:%02x.0" % (getattr(pr, "pci_domain_id", 0), pr.pci_bus_id,
+                                    pr.pci_device_id)
+        info["gpu_pci"] = bus
+        with open(f"/sys/bus/pci/devices/{bus}/numa_node") as f:
+            info["gpu_numa_node"] = int(f.read().strip())
+    except Exception:
+        pass
+    try:
+        ends = {}
+        for line in open("/proc/self/maps"):
+            lo_s, hi_s = line.split()[0].split("-")
+            ends[int(lo_s, 16)] = int(hi_s, 16)
+        maps = open("/proc/self/numa_maps").read().splitlines()
+        out = []
+        for arr in arrays:
+            lo, hi = arr.ctypes.data, arr.ctypes.data + arr.nbytes
+            nodes = {}
+            for line in maps:
+                parts = line.split()
+                start = int(parts[0], 16)
+                if start >= hi or ends.get(start, start) <= lo:
+                    continue
+                for tok in parts[2:]:
+                    k, _, v = tok.partition("=")
+                    if k.startswith("N") and k[1:].isdigit():
+                        nodes[k] = nodes.get(k, 0) + int(v)
+                    elif k == "kernelpagesize_kB":
+                        nodes["page_kB"] = int(v)
+            out.append(nodes)
+        info["buffers"] = out
+    except Exception:
+        pass
+    return info
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -667,7 +716,8 @@ def main():
         out["e2e"] = {"value": flops / (e * 1e-3) / 1e12, "unit": "TFLOP/s",
                       "h2d_bytes_per_step": int(a_host.nbytes + b_host.nbytes),
                       "d2h_bytes_per_step": int(c_host.nbytes), "ms_per_step": e,
-                      "phases_ms": {"h2d": pm[0], "contract": pm[1], "d2h": pm[2]}}
+                      "phases_ms": {"h2d": pm[0], "contract": pm[1], "d2h": pm[2]},
+                      "host": host_placement([a_host, b_host, c_host])}
         if not args.no_cpu:
             A_t = {"data": a_host, "offsets": A.tile_offsets(), "norms": A.norms()}
             B_t = {"data": b_host, "offsets": B.tile_offsets(), "norms": B.norms()}

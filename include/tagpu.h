@@ -221,8 +221,9 @@ typedef struct tagpu_contract_stats {
  * a("b,i,j") * b("b,j,k"), batched outer and Hadamard products included),
  * follow ContEngine's general path: SparseShape::gemm_batched
  * (sparse_shape.h:1707-1885) per fused tile slab, a matrix product per fused
- * element; they run in the plain FP64 form (the emulated form returns
- * TAGPU_ERR_UNSUPPORTED) and need congruent fused and contracted tilings. */
+ * element (in the emulated form, one digit-slice GEMM plan per fused
+ * element, all of them in grouped launches); they need congruent fused and
+ * contracted tilings. */
 tagpu_status tagpu_contract(tagpu_ctx* ctx, const char* c_idx, double alpha,
                             tagpu_array* A, const char* a_idx, tagpu_array* B,
                             const char* b_idx, const tagpu_contract_opts* opts,

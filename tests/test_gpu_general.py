@@ -1,6 +1,8 @@
 """General (fused-index) products on the GPU against the oracle: screened
 shapes bit for bit, integer data exactly (as the reference's tests compare
-against einsum), uniform data within 1e-12 relative Frobenius error."""
+against einsum), uniform data within 1e-12 relative Frobenius error, in the
+plain FP64 form and in the emulated form (one digit-slice GEMM per fused
+element)."""
 import numpy as np
 import pytest
 
@@ -16,14 +18,19 @@ def ta():
     return ta
 
 
+PRECISIONS = [("fp64", 0), ("ozaki", 1)]
+
+
+@pytest.mark.parametrize("prec", PRECISIONS, ids=lambda p: p[0])
 @pytest.mark.parametrize("form", G.FORMS, ids=lambda f: f[0])
-def test_general_product_integer(oracle, ta, world, form):
+def test_general_product_integer(oracle, ta, world, form, prec):
     tag, c, a, b, tra, trb, sparse = form
     ka = G.keep_mask(tra, 1) if sparse else None
     kb = G.keep_mask(trb, 2) if sparse else None
     A, _ = gpu_operand(ta, world, tra, 3, 0, kind=1, keep=ka)
     B, _ = gpu_operand(ta, world, trb, 3, 1, kind=1, keep=kb)
-    C, st = ta.contract(world, c, 1.0, A, a, B, b)
+    precision = ta.PRECISION_OZAKI if prec[1] else ta.PRECISION_FP64
+    C, st = ta.contract(world, c, 1.0, A, a, B, b, precision=precision)
     Ao = oracle_operand(oracle, tra, 3, 0, kind=1, keep=ka)
     Bo = oracle_operand(oracle, trb, 3, 1, kind=1, keep=kb)
     Co, info = oracle.general_contract(c, Ao, a, Bo, b, return_pairs=True)
@@ -34,7 +41,8 @@ def test_general_product_integer(oracle, ta, world, form):
     assert np.array_equal(C.to_dense(C.trange), ref)
 
 
-def test_general_product_uniform_larger(oracle, ta, world):
+@pytest.mark.parametrize("prec", PRECISIONS, ids=lambda p: p[0])
+def test_general_product_uniform_larger(oracle, ta, world, prec):
     """Uneven tiles, several fused tiles and elements, scaled factor and a
     non-canonical target order; uniform data."""
     rng = np.random.default_rng(5)
@@ -48,7 +56,8 @@ def test_general_product_uniform_larger(oracle, ta, world):
     tra, trb = [tb, ti, tj], [tk, tj, tb]
     A, _ = gpu_operand(ta, world, tra, 11, 0, kind=0)
     B, _ = gpu_operand(ta, world, trb, 11, 1, kind=0)
-    C, _ = ta.contract(world, "i,k,b", -0.5, A, "b,i,j", B, "k,j,b")
+    precision = ta.PRECISION_OZAKI if prec[1] else ta.PRECISION_FP64
+    C, _ = ta.contract(world, "i,k,b", -0.5, A, "b,i,j", B, "k,j,b", precision=precision)
     Ao = oracle_operand(oracle, tra, 11, 0, kind=0)
     Bo = oracle_operand(oracle, trb, 11, 1, kind=0)
     Co = oracle.general_contract("i,k,b", Ao, "b,i,j", Bo, "k,j,b", alpha=-0.5)
@@ -62,7 +71,3 @@ def test_general_product_rejections(ta, world):
     with pytest.raises(ta.TAGPUError) as e:   # fused b tiled differently
         ta.contract(world, "b,i,k", 1.0, A, "b,i,j", B, "b,j,k")
     assert e.value.status == 1
-    B2, _ = gpu_operand(ta, world, [G.TB, G.TJ, G.TK], 3, 1, kind=0)
-    with pytest.raises(ta.TAGPUError) as e:   # emulated form: plain FP64 only
-        ta.contract(world, "b,i,k", 1.0, A, "b,i,j", B2, "b,j,k", precision=ta.PRECISION_OZAKI)
-    assert e.value.status == 2

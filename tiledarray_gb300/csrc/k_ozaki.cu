@@ -295,9 +295,11 @@ struct OzParams {
   const int32_t* row_local;
   const int32_t* col_tile;   // N_total
   const int32_t* col_local;
+  const int32_t* msz;
   const int32_t* nsz;
   int64_t Nt;
   const int64_t* coff;       // Mt*Nt result tile offsets
+  int64_t hel;               // fused element: its m x n matrix starts hel * m * n into a tile
   double alpha;
   double* C;
   int64_t M_total, N_total;
@@ -669,7 +671,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
             if (off >= 0) {
               const double v = exact_to_double(hi[j], lo[j], 8 * (TOP - 3),
                                                (2 - 8 * TOP) + (ea - 1022) + (P.EB[gc] - 1022));
-              P.C[off + (int64_t)lr * P.nsz[tj] + P.col_local[gc]] =
+              const int64_t nn = P.nsz[tj];
+              P.C[off + (P.hel * P.msz[ti] + lr) * nn + P.col_local[gc]] =
                   unit_alpha ? v : P.alpha * v;
             }
           }
@@ -705,6 +708,7 @@ struct OperandView {
   const int32_t* rsz;        // tile sizes along rows
   const int32_t* ksz;        // tile sizes along k
   int row_contig;            // 1: element (r, k) at r * 1 + k * rows_in_tile
+  int64_t hel;               // fused element: its matrix starts hel * rows * k into a tile
 };
 
 __device__ __forceinline__ int exp_field(double x) {
@@ -752,7 +756,7 @@ __global__ void __launch_bounds__(256) frame_kernel(const FrameJob* __restrict__
   if (o < 0) return;
   const int m = v.rsz[rt], kk = v.ksz[ktile];
   const int r0 = (int)(q - J.chunk0[rt]) * kFrameRows, r1 = min(m, r0 + kFrameRows);
-  const double* base = v.data + o;
+  const double* base = v.data + o + v.hel * m * kk;
   int32_t* Er = J.E + J.row_start[rt];
   if (v.row_contig) {              // element (r, k) at k * m + r
     const int r = r0 + (threadIdx.x % kFrameRows);
@@ -908,14 +912,18 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 3 : 5) split_kernel(const Sp
     if (staged) {
       for (int t = threadIdx.x; t < nr * nk; t += blockDim.x) {
         const int a = t / nk, b = t - a * nk;
-        s_off[t] = v.off[(int64_t)(rt0 + a) * v.off_stride_row + (int64_t)(kt0 + b) * v.off_stride_k];
+        const int64_t o =
+            v.off[(int64_t)(rt0 + a) * v.off_stride_row + (int64_t)(kt0 + b) * v.off_stride_k];
+        s_off[t] = o < 0 ? o : o + v.hel * v.rsz[rt0 + a] * v.ksz[kt0 + b];
       }
     }
     __syncthreads();
     const double* __restrict__ data = v.data;
-    auto tile_off = [&](int rt, int kt) -> int64_t {
-      return staged ? s_off[(rt - rt0) * nk + (kt - kt0)]
-                    : v.off[(int64_t)rt * v.off_stride_row + (int64_t)kt * v.off_stride_k];
+    // start of the element's matrix in tile (rt, kt), -1 if absent
+    auto tile_off = [&](int rt, int kt, int m, int kk) -> int64_t {
+      if (staged) return s_off[(rt - rt0) * nk + (kt - kt0)];
+      const int64_t o = v.off[(int64_t)rt * v.off_stride_row + (int64_t)kt * v.off_stride_k];
+      return o < 0 ? o : o + v.hel * m * kk;
     };
     double x[EPT];
     if (!v.row_contig) {
@@ -926,7 +934,7 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 3 : 5) split_kernel(const Sp
         const int r = warp + 8 * i, rt = s_rt[r];
         double val = 0.0;
         if (rt >= 0 && kt >= 0) {
-          const int64_t o = tile_off(rt, kt);
+          const int64_t o = tile_off(rt, kt, s_m[r], kk);
           if (o >= 0) val = data[o + (int64_t)s_lr[r] * kk + lk];
         }
         x[i] = val;
@@ -953,7 +961,7 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 3 : 5) split_kernel(const Sp
           const int k = 8 * g + j, kt = s_kt[k];
           double val = 0.0;
           if (rt >= 0 && kt >= 0) {
-            const int64_t o = tile_off(rt, kt);
+            const int64_t o = tile_off(rt, kt, m, s_kk[k]);
             if (o >= 0) val = data[o + (int64_t)s_lk[k] * m + lr];
           }
           x[8 * i + j] = val;
@@ -1440,6 +1448,7 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   a.rsz = v.msz;
   a.ksz = v.ksz;
   a.row_contig = v.a_trans;  // trans: tile stored k x m, rows contiguous
+  a.hel = v.hel;
   OperandView& b = pl->vb;
   b.data = v.B;
   b.off = v.boff;
@@ -1450,6 +1459,7 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   b.rsz = v.nsz;
   b.ksz = v.ksz;
   b.row_contig = v.b_trans ? 0 : 1;  // k x n storage: rows (n) contiguous
+  b.hel = v.hel;
   // brick maps
   int64_t* flag = nullptr;
   int64_t* scan = nullptr;
@@ -1600,9 +1610,11 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   P.row_local = pl->row_local;
   P.col_tile = pl->col_tile;
   P.col_local = pl->col_local;
+  P.msz = v.msz;
   P.nsz = v.nsz;
   P.Nt = v.Nt;
   P.coff = v.coff;
+  P.hel = v.hel;
   P.alpha = v.alpha;
   P.C = v.C;
   P.M_total = pl->M_total;

@@ -1271,7 +1271,9 @@ struct Contraction {
   double* post_in = nullptr;            // GEMM-order result
   double* post_out = nullptr;           // target-order result
   tagpu_contract_stats st{};
-  OzakiPlan* oz = nullptr;              // emulated form scratch
+  // emulated form scratch: one plan per GEMM view (one for an ordinary
+  // contraction, one per fused element for a general product)
+  std::vector<OzakiPlan*> ozs;
   size_t oz_bytes = 0;
   std::string tune_log;
   explicit Contraction(tagpu_ctx* c)
@@ -1279,14 +1281,12 @@ struct Contraction {
         d_coff(c) {}
   ~Contraction();
   tagpu_array* result() { return Cfinal ? Cfinal.get() : C.get(); }
-  bool emulated() const { return precision == TAGPU_PRECISION_OZAKI && oz != nullptr; }
+  bool emulated() const { return precision == TAGPU_PRECISION_OZAKI && !ozs.empty(); }
 };
 
 Contraction::~Contraction() {
-  if (oz) {
-    ozaki_destroy(oz);
-    ctx->used -= oz_bytes;
-  }
+  for (OzakiPlan* pl : ozs) ozaki_destroy(pl);
+  ctx->used -= oz_bytes;
 }
 
 }  // namespace tagpu
@@ -1693,7 +1693,7 @@ tagpu_status build_dmma_items(Contraction& c, int32_t view) {
 // General products: one view per fused element (the slab's tile, pair and
 // result offsets; the element's matrices inside the slab's tiles) and the
 // work items of its nonzero result tiles.
-tagpu_status build_general_items(Contraction& c) {
+tagpu_status build_general_items(Contraction& c, bool with_items) {
   c.items.clear();
   c.gviews.clear();
   const GemmView base = gemm_view(c);
@@ -1708,6 +1708,7 @@ tagpu_status build_general_items(Contraction& c) {
       v.hel = el;
       const int32_t vid = (int32_t)c.gviews.size();
       c.gviews.push_back(v);
+      if (!with_items) continue;
       for (int64_t t = 0; t < MN; ++t) {
         if (c.C->off[h * MN + t] < 0) continue;
         const int64_t i = t / c.Nt, j = t % c.Nt;
@@ -1737,34 +1738,41 @@ tagpu_status plan_all(Contraction& c, const char* c_idx, double alpha, tagpu_arr
   tagpu_status e;
   std::string err;
   if ((e = plan_contraction(c, c_idx, alpha, A, a_idx, B, b_idx, cthr))) return e;
-  if (c.nfused > 0 && c.precision == TAGPU_PRECISION_OZAKI)
-    return fail(ctx, TAGPU_ERR_UNSUPPORTED,
-                "general (fused-index) products run in the plain FP64 form only");
   if ((e = run_shape_and_pairs(c))) return e;
   if ((e = make_result(c, A, B))) return e;
   if ((e = prepare_operands(c, A, B))) return e;
   c.view = gemm_view(c);
-  if (c.nfused > 0) {
-    if ((e = build_general_items(c))) return e;
-  } else if (c.precision == TAGPU_PRECISION_OZAKI && c.npairs > 0 && c.C->elements > 0) {
-    e = ozaki_plan(ctx->stream, c.view, c.msz.data(), c.nsz.data(), c.ksz.data(), c.slices,
-                   &c.oz, &err);
-    if (e) return fail(ctx, e, "%s", err.c_str());
-    c.oz_bytes = ozaki_scratch_bytes(c.oz);
-    ctx->used += c.oz_bytes;
+  const bool emul = c.precision == TAGPU_PRECISION_OZAKI && c.npairs > 0 && c.C->elements > 0;
+  if (c.nfused > 0 && (e = build_general_items(c, !emul))) return e;
+  if (emul) {
+    // one plan per GEMM view: the contraction, or every fused element of a
+    // general product (its matrices inside the slab's tiles)
+    const std::vector<GemmView> one(1, c.view);
+    const std::vector<GemmView>& vs = c.nfused > 0 ? c.gviews : one;
+    c.st.gemm_blocks = 0;
+    for (const GemmView& v : vs) {
+      OzakiPlan* pl = nullptr;
+      e = ozaki_plan(ctx->stream, v, c.msz.data(), c.nsz.data(), c.ksz.data(), c.slices, &pl,
+                     &err);
+      if (e) return fail(ctx, e, "%s", err.c_str());
+      c.ozs.push_back(pl);
+      const size_t b = ozaki_scratch_bytes(pl);
+      c.oz_bytes += b;
+      ctx->used += b;
+      c.st.gemm_blocks += 2 * ozaki_units(pl);   // a unit is a pair of output blocks
+      if (ctx->budget && ctx->used.load() > ctx->budget)
+        return fail(ctx, TAGPU_ERR_NOMEM, "emulated-form scratch (%zu bytes) exceeds the budget",
+                    c.oz_bytes);
+    }
     const char* env_tune = getenv("TAGPU_AUTOTUNE");
-    if ((opts && opts->autotune) || (env_tune && atoi(env_tune) != 0)) {
+    if (c.ozs.size() == 1 && ((opts && opts->autotune) || (env_tune && atoi(env_tune) != 0))) {
       std::string log;
       const char* cache = getenv("TAGPU_TUNE_CACHE");
-      e = ozaki_autotune(c.oz, ctx->sm_count, ctx->stream, cache, &log, &err);
+      e = ozaki_autotune(c.ozs[0], ctx->sm_count, ctx->stream, cache, &log, &err);
       if (e) return fail(ctx, e, "%s", err.c_str());
       c.tune_log = log;
     }
-    if (ctx->budget && ctx->used.load() > ctx->budget)
-      return fail(ctx, TAGPU_ERR_NOMEM, "emulated-form scratch (%zu bytes) exceeds the budget",
-                  c.oz_bytes);
-    c.st.gemm_blocks = 2 * ozaki_units(c.oz);   // a unit is a pair of output blocks
-  } else {
+  } else if (c.nfused == 0) {
     if ((e = build_dmma_items(c, 0))) return e;
   }
   if (c.post) {
@@ -1869,21 +1877,21 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, Launch
   // emulated form: frames and splitting per contraction, then one GEMM launch
   // per slice count over the output blocks of all of them
   lb.err_owners.clear();
-  std::vector<Contraction*> by_s[8];
+  std::vector<OzakiPlan*> by_s[8];
   for (auto* c : cs) {
     if (!c->emulated()) continue;
-    by_s[ozaki_slices(c->oz)].push_back(c);
+    for (OzakiPlan* pl : c->ozs) by_s[ozaki_slices(pl)].push_back(pl);
     c->st.gemm_launches = 5;
   }
   // frames and splits: row-chunked plans and lone plans on their own, the
   // rest of each digit count in one launch per step
   for (int S = 2; S < 8; ++S) {
     std::vector<OzakiPlan*> grp;
-    for (auto* c : by_s[S]) {
-      if (ozaki_chunks(c->oz) > 1)
-        ozaki_enqueue(c->oz, ctx->sm_count, stream);
+    for (OzakiPlan* pl : by_s[S]) {
+      if (ozaki_chunks(pl) > 1)
+        ozaki_enqueue(pl, ctx->sm_count, stream);
       else
-        grp.push_back(c->oz);
+        grp.push_back(pl);
     }
     if (grp.size() == 1) ozaki_enqueue(grp[0], ctx->sm_count, stream);
     if (grp.size() < 2) continue;
@@ -1900,20 +1908,19 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, Launch
                         ctx->sm_count, stream);
   }
   for (int S = 2; S < 8; ++S) {
-    auto& g0 = by_s[S];
-    std::vector<Contraction*> g;
-    for (auto* c : g0) {
-      if (ozaki_chunks(c->oz) > 1) {
-        ozaki_enqueue_gemm(c->oz, ctx->sm_count, stream);
-        lb.err_owners.push_back(c->oz);
+    std::vector<OzakiPlan*> g;
+    for (OzakiPlan* pl : by_s[S]) {
+      if (ozaki_chunks(pl) > 1) {
+        ozaki_enqueue_gemm(pl, ctx->sm_count, stream);
+        lb.err_owners.push_back(pl);
       } else {
-        g.push_back(c);
+        g.push_back(pl);
       }
     }
     if (g.empty()) continue;
-    lb.err_owners.push_back(g[0]->oz);
+    lb.err_owners.push_back(g[0]);
     if (g.size() == 1) {
-      ozaki_enqueue_gemm(g[0]->oz, ctx->sm_count, stream);
+      ozaki_enqueue_gemm(g[0], ctx->sm_count, stream);
       continue;
     }
     if (upload) {
@@ -1921,8 +1928,8 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, Launch
       std::vector<uint8_t> params(psz * g.size());
       std::vector<int64_t> vstart(1, 0);
       for (size_t i = 0; i < g.size(); ++i) {
-        ozaki_params(g[i]->oz, params.data() + i * psz);
-        vstart.push_back(vstart.back() + ozaki_units(g[i]->oz));
+        ozaki_params(g[i], params.data() + i * psz);
+        vstart.push_back(vstart.back() + ozaki_units(g[i]));
       }
       tagpu_status e;
       if ((e = upload_vec(ctx, lb.ozp[S], params)) || (e = upload_vec(ctx, lb.ozv[S], vstart)))
@@ -1931,7 +1938,7 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, Launch
       if (stream != ctx->stream) CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     }
     ozaki_enqueue_gemm_views(lb.ozp[S].p, lb.ozv[S].as<int64_t>(), (int)g.size(), lb.oz_nblk[S],
-                             S, ozaki_error_flag(g[0]->oz), ctx->sm_count, stream);
+                             S, ozaki_error_flag(g[0]), ctx->sm_count, stream);
   }
   if (!items.empty()) {
     launch_dmma_gemm(stream, d_views.as<GemmView>(), d_items.as<WorkItem>(),
@@ -1959,12 +1966,23 @@ tagpu_status contract_impl(tagpu_ctx* ctx, const char* c_idx, double alpha, tagp
   if (e) return e;
   LaunchBufs lbuf(ctx);
   std::vector<Contraction*> cs{&c};
-  if (c.emulated()) {
+  if (c.emulated() && c.ozs.size() > 1) {
+    // general product: the fused elements' plans in grouped launches
+    EventTimer tm(ctx->stream);
+    if ((e = enqueue_gemms(ctx, cs, lbuf, true))) return e;
+    tm.stop();
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    c.st.ms_gemm = tm.ms();
+    if (lbuf.any_error())
+      return fail(ctx, TAGPU_ERR_TIMEOUT,
+                  "emulated GEMM: a bounded wait ran out; results invalid");
+  } else if (c.emulated()) {
+    OzakiPlan* oz = c.ozs[0];
     EventTimer t_split(ctx->stream);
-    ozaki_enqueue(c.oz, ctx->sm_count, ctx->stream);
+    ozaki_enqueue(oz, ctx->sm_count, ctx->stream);
     t_split.stop();
     EventTimer t_gemm(ctx->stream);
-    ozaki_enqueue_gemm(c.oz, ctx->sm_count, ctx->stream);
+    ozaki_enqueue_gemm(oz, ctx->sm_count, ctx->stream);
     t_gemm.stop();
     if (c.post) c.post->enqueue(ctx->stream, c.post_in, c.post_out);
     CUDA_TRY(ctx, cudaGetLastError());
@@ -1972,7 +1990,7 @@ tagpu_status contract_impl(tagpu_ctx* ctx, const char* c_idx, double alpha, tagp
     c.st.ms_split = t_split.ms();
     c.st.ms_gemm = t_gemm.ms();
     c.st.gemm_launches = 5;
-    const int oe = ozaki_error(c.oz);
+    const int oe = ozaki_error(oz);
     if (oe)
       return fail(ctx, TAGPU_ERR_TIMEOUT,
                   "emulated GEMM: a bounded wait ran out (role code %d); results invalid", oe);
