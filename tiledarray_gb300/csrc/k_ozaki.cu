@@ -21,7 +21,8 @@
 //    ranges and the B slices adjacent in shared memory, so the pairs of one
 //    p form a single MMA of N = 64 * (S + 1 - p) (two above 256).  Every
 //    product is an integer below 2^14.  Level t (t-1 products per k)
-//    restarts from zero every 32/(t-1) stages of 32 k, so levels 2..5 stay
+//    restarts from zero every 32, 16, 8, 8 stages of 32 k (t = 2..5; a power
+//    of two <= 32/(t-1), so restarts coincide), so levels 2..5 stay
 //    at or below 2^24 where every fp32 sum of integers is exact; levels 6
 //    and 7 (weight 2^-32 and 2^-40 against level 2) sum over the whole
 //    output block in fp32, a rounding below 2^-41 of sum_k |a b|;
@@ -58,16 +59,21 @@ constexpr int BM = 128;            // output block rows (MMA M)
 constexpr int BN = 64;             // output block columns (MMA N)
 constexpr int BK = 32;             // k per stage (two MMA K = 16 steps)
 // Level t collects t-1 digit products |d e| <= 2^14 per k.  Levels up to
-// kExactTop are kept exact: level t restarts from zero every
-// drain_period(t) = 32 / (t-1) stages (32 k each), so it never exceeds
-// (t-1) * 32 * drain_period(t) * 2^14 <= 2^24, where every fp32 sum of
-// integers is exact.  Levels above kExactTop (weight 2^-32 and below against
-// level 2) accumulate over the whole output block in fp32 and are read once;
-// their rounding stays below 2^-41 of sum_k |a_ik b_kj| per element, under
-// FP64 GEMM's own worst-case bound.  The schedule is a fixed function of the
-// stage index, so results do not depend on block order or row chunking.
+// kExactTop are kept exact: level t restarts from zero every drain_period(t)
+// stages (32 k each), the largest power of two <= 32 / (t-1) (32, 16, 8, 8
+// for t = 2..5), so it never exceeds (t-1) * 32 * drain_period(t) * 2^14
+// <= 2^24, where every fp32 sum of integers is exact.  Powers of two make
+// the restarts of different levels fall on the same stages (every 8th), so
+// the MMA warp waits for the epilogue at one stage in 8.  Levels above
+// kExactTop (weight 2^-32 and below against level 2) accumulate over the
+// whole output block in fp32 and are read once; their rounding stays below
+// 2^-41 of sum_k |a_ik b_kj| per element, under FP64 GEMM's own worst-case
+// bound.  The schedule is a fixed function of the stage index, so results do
+// not depend on block order or row chunking.
 constexpr int kExactTop = 5;
-__host__ __device__ constexpr int drain_period(int t) { return 32 / (t - 1); }
+__host__ __device__ constexpr int drain_period(int t) {
+  return t <= 2 ? 32 : t == 3 ? 16 : t <= 5 ? 8 : t <= 9 ? 4 : t <= 17 ? 2 : 1;
+}
 // Bit t set: level t (2..TOP) starts from zero at stage x of an output block.
 template <int TOP>
 __device__ __forceinline__ uint32_t restart_mask(int64_t x) {
