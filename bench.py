@@ -128,6 +128,12 @@ def host_placement(arrays, device=0):
     (from /proc/self/numa_maps), the NUMA node of the GPU's PCI function,
     and the CPUs and memory nodes this process may use."""
     info = {"cpus": len(os.sched_getaffinity(0))}
+    for k in ("enabled", "defrag"):
+        try:
+            with open(f"/sys/kernel/mm/transparent_hugepage/{k}") as f:
+                info["thp_" + k] = f.read().strip()
+        except OSError:
+            pass
     try:
         for line in open("/proc/self/status"):
             if line.startswith("Mems_allowed_list:"):
@@ -698,9 +704,11 @@ def main():
         c_host = w.host_array(C2.info().elements)
         del C2
         e2e_ms, parts = [], []
+        iters = []
         for _ in range(max(1, min(args.steps, 3))):
             t0 = time.perf_counter()
             A.upload(a_host)
+            ta_ = time.perf_counter()
             B.upload(b_host)
             t1 = time.perf_counter()
             C2, st2 = step()
@@ -710,6 +718,8 @@ def main():
             t3 = time.perf_counter()
             e2e_ms.append((t3 - t0) * 1e3)
             parts.append(((t1 - t0) * 1e3, (t2 - t1) * 1e3, (t3 - t2) * 1e3))
+            iters.append([round((ta_ - t0) * 1e3, 2), round((t1 - ta_) * 1e3, 2),
+                          round((t2 - t1) * 1e3, 2), round((t3 - t2) * 1e3, 2)])
             del C2
         e = statistics.median(e2e_ms)
         pm = parts[e2e_ms.index(e)] if e in e2e_ms else parts[0]
@@ -717,7 +727,32 @@ def main():
                       "h2d_bytes_per_step": int(a_host.nbytes + b_host.nbytes),
                       "d2h_bytes_per_step": int(c_host.nbytes), "ms_per_step": e,
                       "phases_ms": {"h2d": pm[0], "contract": pm[1], "d2h": pm[2]},
+                      "iters_ms": iters,   # per step: upload A, upload B, contract, download
                       "host": host_placement([a_host, b_host, c_host])}
+        # the host link itself, outside the timed region: one 2 GB-class copy
+        # each way from the library buffer and from a torch-pinned buffer
+        import torch
+        link = {}
+        dev_t = torch.empty(a_host.size, dtype=torch.float64, device="cuda")
+        pin_t = torch.empty(a_host.size, dtype=torch.float64, pin_memory=True)
+        pin_t.fill_(0.5)
+        for name, host_t in (("library", torch.from_numpy(a_host)), ("torch_pinned", pin_t)):
+            for rep in range(2):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                dev_t.copy_(host_t, non_blocking=True)
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                host_t.copy_(dev_t, non_blocking=True)
+                torch.cuda.synchronize()
+                t2 = time.perf_counter()
+            link[name] = {"h2d_GBs": a_host.nbytes / (t1 - t0) / 1e9,
+                          "d2h_GBs": a_host.nbytes / (t2 - t1) / 1e9}
+        t0 = time.perf_counter()
+        A.upload(a_host)
+        link["upload_A_ms_after"] = (time.perf_counter() - t0) * 1e3
+        out["e2e"]["host_link"] = link
+        del dev_t, pin_t
         if not args.no_cpu:
             A_t = {"data": a_host, "offsets": A.tile_offsets(), "norms": A.norms()}
             B_t = {"data": b_host, "offsets": B.tile_offsets(), "norms": B.norms()}

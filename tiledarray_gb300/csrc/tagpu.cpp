@@ -919,28 +919,6 @@ std::unordered_map<void*, HostMap>& host_maps() {
   static std::unordered_map<void*, HostMap> m;
   return m;
 }
-// Transparent huge page size if the kernel offers them to madvise, else 0.
-size_t host_huge_page() {
-  static size_t sz = [] {
-    size_t v = 0;
-    if (FILE* f = fopen("/sys/kernel/mm/transparent_hugepage/enabled", "r")) {
-      char buf[128] = {0};
-      const size_t n = fread(buf, 1, sizeof(buf) - 1, f);
-      fclose(f);
-      buf[n] = 0;
-      if (!strstr(buf, "[never]")) {
-        if (FILE* g = fopen("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size", "r")) {
-          unsigned long long x = 0;
-          if (fscanf(g, "%llu", &x) == 1 && x >= 4096 && x <= (1ull << 30) && !(x & (x - 1)))
-            v = (size_t)x;
-          fclose(g);
-        }
-      }
-    }
-    return v;
-  }();
-  return sz;
-}
 constexpr char kArchiveMagic[8] = {'T', 'A', 'G', 'P', 'U', 'A', 'R', 'R'};
 constexpr size_t kStage = size_t(64) << 20;
 
@@ -969,32 +947,31 @@ struct File {
 
 extern "C" {
 
-// Host buffers: an anonymous mapping aligned to the transparent huge page
-// size, advised to use huge pages, touched and registered with CUDA, so the
-// GPU reaches it through few, large translations; cudaHostAlloc where that
-// is not available.  The mapping of each buffer is remembered for the free.
+// Host buffers: an anonymous mapping kept out of transparent huge pages,
+// touched and registered with CUDA; cudaHostAlloc where that fails.  With
+// huge pages advised, host-to-device copies from freshly allocated buffers
+// ran at a few GB/s for seconds in some runs before reaching ~210 GB/s (as
+// if the kernel were still collapsing the mapping into huge pages); base
+// pages reach the same ~210 GB/s.  The mapping of each buffer is remembered
+// for the free.
 tagpu_status tagpu_host_alloc(tagpu_ctx* ctx, size_t bytes, void** p) {
   if (!ctx || !p) return TAGPU_ERR_INVALID;
   *p = nullptr;
   cudaSetDevice(ctx->device);
   if (bytes == 0) return TAGPU_OK;
-  const size_t huge = host_huge_page();
-  if (huge) {
-    const size_t len = (bytes + huge - 1) / huge * huge;
-    void* m = mmap(nullptr, len + huge, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1,
-                   0);
+  {
+    void* m = mmap(nullptr, bytes, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
     if (m != MAP_FAILED) {
-      uint8_t* a = (uint8_t*)(((uintptr_t)m + huge - 1) & ~(uintptr_t)(huge - 1));
-      madvise(a, len, MADV_HUGEPAGE);
-      memset(a, 0, len);
-      if (cudaHostRegister(a, len, cudaHostRegisterDefault) == cudaSuccess) {
+      madvise(m, bytes, MADV_NOHUGEPAGE);
+      memset(m, 0, bytes);
+      if (cudaHostRegister(m, bytes, cudaHostRegisterDefault) == cudaSuccess) {
         std::lock_guard<std::mutex> lk(host_maps_mu());
-        host_maps()[a] = HostMap{m, len + huge, true};
-        *p = a;
+        host_maps()[m] = HostMap{m, bytes, true};
+        *p = m;
         return TAGPU_OK;
       }
       cudaGetLastError();
-      munmap(m, len + huge);
+      munmap(m, bytes);
     }
   }
   const cudaError_t e = cudaHostAlloc(p, bytes, cudaHostAllocDefault);
