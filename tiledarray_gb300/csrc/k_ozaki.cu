@@ -48,6 +48,7 @@
 #include <cstdlib>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "internal.h"
@@ -835,6 +836,7 @@ __device__ __forceinline__ void split_digits(double x, int frame, uint32_t (&h)[
 struct SplitJob {
   OperandView v;
   const int32_t *row_tile, *row_local, *k_tile, *k_local;
+  const int32_t *row_ext, *k_ext;   // extent of the tile holding each fused row / k
   const int32_t* E;           // frames of the operand's fused rows
   int64_t rows_total, k_total;
   const int32_t* bricks;      // nbricks x 2 (row block, k block)
@@ -894,11 +896,10 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 3 : 5) split_kernel(const Sp
     for (int i = threadIdx.x; i < ROWS; i += blockDim.x) {
       const int64_t gr = r0 + i;
       if (gr < rows_total) {
-        const int rt = J.row_tile[gr];
-        s_rt[i] = rt;
+        s_rt[i] = J.row_tile[gr];
         s_lr[i] = J.row_local[gr];
         s_fr[i] = J.E[gr];
-        s_m[i] = v.rsz[rt];
+        s_m[i] = J.row_ext[gr];
       } else {
         s_rt[i] = -1;
         s_fr[i] = 0;
@@ -907,10 +908,9 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 3 : 5) split_kernel(const Sp
     if (threadIdx.x < BK) {
       const int64_t gk = k0 + threadIdx.x;
       if (gk < k_total) {
-        const int kt = J.k_tile[gk];
-        s_kt[threadIdx.x] = kt;
+        s_kt[threadIdx.x] = J.k_tile[gk];
         s_lk[threadIdx.x] = J.k_local[gk];
-        s_kk[threadIdx.x] = v.ksz[kt];
+        s_kk[threadIdx.x] = J.k_ext[gk];
       } else {
         s_kt[threadIdx.x] = -1;
       }
@@ -920,31 +920,66 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 3 : 5) split_kernel(const Sp
         const int a = t / nk, b = t - a * nk;
         const int64_t o =
             v.off[(int64_t)(rt0 + a) * v.off_stride_row + (int64_t)(kt0 + b) * v.off_stride_k];
-        s_off[t] = o < 0 ? o : o + v.hel * v.rsz[rt0 + a] * v.ksz[kt0 + b];
+        s_off[t] = o < 0 || v.hel == 0 ? o : o + v.hel * v.rsz[rt0 + a] * v.ksz[kt0 + b];
       }
     }
     __syncthreads();
     const double* __restrict__ data = v.data;
-    // start of the element's matrix in tile (rt, kt), -1 if absent
-    auto tile_off = [&](int rt, int kt, int m, int kk) -> int64_t {
-      if (staged) return s_off[(rt - rt0) * nk + (kt - kt0)];
-      const int64_t o = v.off[(int64_t)rt * v.off_stride_row + (int64_t)kt * v.off_stride_k];
-      return o < 0 ? o : o + v.hel * m * kk;
-    };
     double x[EPT];
-    if (!v.row_contig) {
-      // element (r, k) at o + lr * kk + lk: lanes along k, rows warp + 8 i
-      const int k = lane, kt = s_kt[k], lk = s_lk[k], kk = kt >= 0 ? s_kk[k] : 0;
-#pragma unroll
-      for (int i = 0; i < EPT; ++i) {
-        const int r = warp + 8 * i, rt = s_rt[r];
-        double val = 0.0;
-        if (rt >= 0 && kt >= 0) {
-          const int64_t o = tile_off(rt, kt, s_m[r], kk);
-          if (o >= 0) val = data[o + (int64_t)s_lr[r] * kk + lk];
+    // All loads of the thread, with the tile offsets from shared memory
+    // (ST) or looked up per element; two instantiations, so the staged path
+    // carries no global offset loads.
+    auto load_all = [&](auto st_c) {
+      constexpr bool ST = decltype(st_c)::value;
+      // start of the element's matrix in tile (rt, kt), -1 if absent
+      auto tile_off = [&](int rt, int kt, int m, int kk) -> int64_t {
+        if constexpr (ST) {
+          return s_off[(rt - rt0) * nk + (kt - kt0)];
+        } else {
+          const int64_t o =
+              v.off[(int64_t)rt * v.off_stride_row + (int64_t)kt * v.off_stride_k];
+          return o < 0 ? o : o + v.hel * m * kk;
         }
-        x[i] = val;
+      };
+      if (!v.row_contig) {
+        // element (r, k) at o + lr * kk + lk: lanes along k, rows warp + 8 i
+        const int k = lane, kt = s_kt[k], lk = s_lk[k], kk = kt >= 0 ? s_kk[k] : 0;
+#pragma unroll
+        for (int i = 0; i < EPT; ++i) {
+          const int r = warp + 8 * i, rt = s_rt[r];
+          double val = 0.0;
+          if (rt >= 0 && kt >= 0) {
+            const int64_t o = tile_off(rt, kt, ST ? 0 : s_m[r], kk);
+            if (o >= 0) val = data[o + (int64_t)s_lr[r] * kk + lk];
+          }
+          x[i] = val;
+        }
+      } else {
+        // element (r, k) at o + lk * m + lr: a thread owns row r = 32 (item /
+        // 4) + lane and the eight k of group item % 4
+#pragma unroll
+        for (int i = 0; i < EPT / 8; ++i) {
+          const int item = warp + 8 * i, r = (item >> 2) * 32 + lane, g = item & 3;
+          const int rt = s_rt[r], lr = s_lr[r], m = s_m[r];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int k = 8 * g + j, kt = s_kt[k];
+            double val = 0.0;
+            if (rt >= 0 && kt >= 0) {
+              const int64_t o = tile_off(rt, kt, m, ST ? 0 : s_kk[k]);
+              if (o >= 0) val = data[o + (int64_t)s_lk[k] * m + lr];
+            }
+            x[8 * i + j] = val;
+          }
+        }
       }
+    };
+    if (staged)
+      load_all(std::true_type{});
+    else
+      load_all(std::false_type{});
+    if (!v.row_contig) {
+      const int k = lane;
       uint8_t* c0 = img + stage_chunk<ROWS>(0, k >> 3) + (k & 7) * 2;
 #pragma unroll
       for (int i = 0; i < EPT; ++i) {
@@ -956,23 +991,6 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 3 : 5) split_kernel(const Sp
           *reinterpret_cast<uint16_t*>(c0 + r * 16 + p * SPAD) = (uint16_t)h[p];
       }
     } else {
-      // element (r, k) at o + lk * m + lr: a thread owns row r = 32 (item / 4)
-      // + lane and the eight k of group item % 4
-#pragma unroll
-      for (int i = 0; i < EPT / 8; ++i) {
-        const int item = warp + 8 * i, r = (item >> 2) * 32 + lane, g = item & 3;
-        const int rt = s_rt[r], lr = s_lr[r], m = s_m[r];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int k = 8 * g + j, kt = s_kt[k];
-          double val = 0.0;
-          if (rt >= 0 && kt >= 0) {
-            const int64_t o = tile_off(rt, kt, m, s_kk[k]);
-            if (o >= 0) val = data[o + (int64_t)s_lk[k] * m + lr];
-          }
-          x[8 * i + j] = val;
-        }
-      }
 #pragma unroll
       for (int i = 0; i < EPT / 8; ++i) {
         const int item = warp + 8 * i, r = (item >> 2) * 32 + lane, g = item & 3;
@@ -1171,6 +1189,7 @@ struct OzakiPlan {
   std::vector<DevVec> bufs;
   int32_t *row_tile = nullptr, *row_local = nullptr, *k_tile = nullptr, *k_local = nullptr,
           *col_tile = nullptr, *col_local = nullptr, *rstart = nullptr, *cstart = nullptr;
+  int32_t *row_ext = nullptr, *k_ext = nullptr, *col_ext = nullptr;   // tile extent per index
   int4* blk_ab = nullptr;
   int32_t *EA = nullptr, *EB = nullptr, *brickA = nullptr, *brickB = nullptr, *listA = nullptr,
           *listB = nullptr, *blk = nullptr, *blk_kb = nullptr;
@@ -1239,17 +1258,36 @@ template <int S>
 void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int64_t nblk,
                    int* err, int sm_count, cudaStream_t st) {
   const size_t smem = Smem<S>::kBytes;
-  // the shared-memory attribute is per device
+  // the shared-memory attribute and the co-resident cluster count are per
+  // device
   static bool set[kMaxDevices] = {};
+  static int clusters[kMaxDevices] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < kMaxDevices && !set[dev]) {
+  if (dev < 0 || dev >= kMaxDevices) dev = 0;
+  if (!set[dev]) {
     cudaFuncSetAttribute(ozaki_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
+    // A persistent grid larger than what fits at once would leave the extra
+    // clusters to start after others finish their whole share.
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(2 * (sm_count / 2)), 1, 1);
+    cfg.blockDim = dim3(THREADS, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, ozaki_gemm_kernel<S>, &cfg) != cudaSuccess || n <= 0) {
+      cudaGetLastError();
+      n = sm_count / 2;
+    }
+    clusters[dev] = std::min(n, sm_count / 2);
     set[dev] = true;
+    if (const char* e = getenv("TAGPU_VERBOSE"))
+      if (atoi(e) > 0)
+        fprintf(stderr, "tagpu: emulated GEMM (S=%d) on device %d: %d co-resident clusters of 2 "
+                "(%d SMs)\n", S, dev, n, sm_count);
   }
   // clusters of two CTAs, one unit (pair of output blocks) at a time each
-  const int64_t grid = 2 * std::min<int64_t>(nblk, sm_count / 2);
+  const int64_t grid = 2 * std::min<int64_t>(nblk, clusters[dev]);
   if (grid > 0) {
     ozaki_gemm_kernel<S><<<(unsigned)grid, THREADS, smem, st>>>(views, vstart, nviews, nblk, err);
     count_launch();
@@ -1435,7 +1473,16 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   pl->RB = (pl->M_total + BM - 1) / BM;
   pl->CB = (pl->N_total + BN - 1) / BN;
   pl->KB = (pl->K_total + BK - 1) / BK;
+  auto extents = [](const std::vector<int32_t>& tile, const int32_t* sz) {
+    std::vector<int32_t> e(tile.size());
+    for (size_t i = 0; i < tile.size(); ++i) e[i] = sz[tile[i]];
+    return e;
+  };
   tagpu_status st;
+  if ((st = pl->upload(&pl->row_ext, extents(rt, h_msz), err)) ||
+      (st = pl->upload(&pl->k_ext, extents(kt_, h_ksz), err)) ||
+      (st = pl->upload(&pl->col_ext, extents(ct, h_nsz), err)))
+    return st;
   if ((st = pl->upload(&pl->row_tile, rt, err)) || (st = pl->upload(&pl->row_local, rl, err)) ||
       (st = pl->upload(&pl->rstart, rs, err)) || (st = pl->upload(&pl->k_tile, kt_, err)) ||
       (st = pl->upload(&pl->k_local, kl, err)) || (st = pl->upload(&pl->col_tile, ct, err)) ||
@@ -1638,14 +1685,15 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
     return st;
   pl->h_frames[0] = FrameJob{pl->va, pl->rstart, pl->chunk0_a, pl->EA, 0};
   pl->h_frames[1] = FrameJob{pl->vb, pl->cstart, pl->chunk0_b, pl->EB, pl->frame_items_a};
-  pl->h_split_b = SplitJob{pl->vb,     pl->col_tile, pl->col_local, pl->k_tile,
-                           pl->k_local, pl->EB,      pl->N_total,   pl->K_total,
-                           pl->listB,  pl->nB,      pl->Bpack,     0};
+  pl->h_split_b = SplitJob{pl->vb,      pl->col_tile, pl->col_local, pl->k_tile,
+                           pl->k_local, pl->col_ext,  pl->k_ext,     pl->EB,
+                           pl->N_total, pl->K_total,  pl->listB,     pl->nB,
+                           pl->Bpack,   0};
   pl->h_split_a.clear();
   for (int c = 0; c < pl->nchunk; ++c)
     pl->h_split_a.push_back(SplitJob{pl->va, pl->row_tile, pl->row_local, pl->k_tile,
-                                     pl->k_local, pl->EA, pl->M_total, pl->K_total,
-                                     pl->listA + 2 * pl->chunk_slot[c],
+                                     pl->k_local, pl->row_ext, pl->k_ext, pl->EA, pl->M_total,
+                                     pl->K_total, pl->listA + 2 * pl->chunk_slot[c],
                                      pl->chunk_slot[c + 1] - pl->chunk_slot[c], pl->Apack, 0});
   {
     const std::vector<FrameJob> fj(pl->h_frames, pl->h_frames + 2);
