@@ -338,3 +338,24 @@ def test_host_buffers_roundtrip(ta, world):
     out = world.host_array(n)
     world.check(world.L.tagpu_array_download(B.h, out.ctypes.data_as(ta._f64p), n))
     assert np.array_equal(out, A.download())
+
+
+@pytest.mark.parametrize("shift", [0, 1, 3])
+def test_host_buffers_unaligned(ta, world, shift):
+    """Registered host memory at offsets of 0, 1 and 3 doubles: the
+    kernel-driven copies take their 16-byte and 8-byte paths, move every
+    element both ways and write nothing outside the buffer."""
+    A, _ = gpu_operand(ta, world, [[0, 40, 101], [0, 64, 93]], 4, 0, kind=0)
+    n = A.info().elements
+    base = world.host_array(n + 4)
+    view = base[shift:shift + n]
+    view[:] = A.download()
+    B = ta.DistArray(world, A.trange)
+    B.set_shape(A.norms(), do_not_scale=True, threshold=A.info().threshold)
+    world.check(world.L.tagpu_array_upload(B.h, view.ctypes.data_as(ta._f64p), n))
+    assert np.array_equal(B.download(), A.download())
+    back = world.host_array(n + 4)
+    back[:] = -1.0
+    world.check(world.L.tagpu_array_download(B.h, back[shift:].ctypes.data_as(ta._f64p), n))
+    assert np.array_equal(back[shift:shift + n], A.download())
+    assert np.all(back[:shift] == -1.0) and np.all(back[shift + n:] == -1.0)

@@ -22,7 +22,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["k_shape.cu", "k_permute.cu", "k_add.cu", "k_gen.cu", "k_dmma.cu", "k_ozaki.cu",
+CU_SOURCES = ["k_shape.cu", "k_permute.cu", "k_add.cu", "k_copy.cu", "k_gen.cu", "k_dmma.cu", "k_ozaki.cu",
               "k_noalloc.cu", "k_peak.cu"]
 CPP_SOURCES = ["tagpu.cpp"]
 

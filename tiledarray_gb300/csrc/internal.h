@@ -56,6 +56,11 @@ struct PermuteDesc {
 struct AddChunk {
   int64_t r, c, p, len;
 };
+// Host <-> device copy of array storage by a kernel over a coherent host
+// link; usable when `host` is registered host memory whose address the
+// device can dereference on a platform that shares the host page tables.
+bool link_copy_usable(const void* host);
+void launch_link_copy(cudaStream_t s, void* dst, const void* src, size_t bytes);
 void launch_add_tiles(cudaStream_t s, const AddChunk* chunks, int64_t nchunks, const double* C,
                       const double* P, double* R);
 

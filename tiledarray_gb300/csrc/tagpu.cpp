@@ -644,9 +644,14 @@ tagpu_status tagpu_array_upload(tagpu_array* a, const double* tiles, int64_t n) 
   pack_offsets(a);
   tagpu_status st = ensure_storage(a);
   if (st) return st;
-  if (n)
-    CUDA_TRY(ctx, cudaMemcpyAsync(a->data, tiles, n * sizeof(double), cudaMemcpyHostToDevice,
-                                  ctx->stream));
+  if (n) {
+    if (link_copy_usable(tiles))
+      launch_link_copy(ctx->stream, a->data, tiles, n * sizeof(double));
+    else
+      CUDA_TRY(ctx, cudaMemcpyAsync(a->data, tiles, n * sizeof(double), cudaMemcpyHostToDevice,
+                                    ctx->stream));
+  }
+  CUDA_TRY(ctx, cudaGetLastError());
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return TAGPU_OK;
 }
@@ -660,9 +665,14 @@ tagpu_status tagpu_array_download(const tagpu_array* a, double* tiles, int64_t n
     return fail(ctx, TAGPU_ERR_INVALID, "download: buffer holds %lld elements, array %lld",
                 (long long)n, (long long)a->elements);
   if (n && !tiles) return fail(ctx, TAGPU_ERR_INVALID, "download: null buffer");
-  if (n)
-    CUDA_TRY(ctx, cudaMemcpyAsync(tiles, a->data, n * sizeof(double), cudaMemcpyDeviceToHost,
-                                  ctx->stream));
+  if (n) {
+    if (link_copy_usable(tiles))
+      launch_link_copy(ctx->stream, tiles, a->data, n * sizeof(double));
+    else
+      CUDA_TRY(ctx, cudaMemcpyAsync(tiles, a->data, n * sizeof(double), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+  }
+  CUDA_TRY(ctx, cudaGetLastError());
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return TAGPU_OK;
 }
@@ -947,13 +957,9 @@ struct File {
 
 extern "C" {
 
-// Host buffers: an anonymous mapping kept out of transparent huge pages,
-// touched and registered with CUDA; cudaHostAlloc where that fails.  With
-// huge pages advised, host-to-device copies from freshly allocated buffers
-// ran at a few GB/s for seconds in some runs before reaching ~210 GB/s (as
-// if the kernel were still collapsing the mapping into huge pages); base
-// pages reach the same ~210 GB/s.  The mapping of each buffer is remembered
-// for the free.
+// Host buffers: an anonymous mapping on base pages (huge pages gave the host
+// link no measurable gain), touched and registered with CUDA; cudaHostAlloc
+// where that fails.  The mapping of each buffer is remembered for the free.
 tagpu_status tagpu_host_alloc(tagpu_ctx* ctx, size_t bytes, void** p) {
   if (!ctx || !p) return TAGPU_ERR_INVALID;
   *p = nullptr;
