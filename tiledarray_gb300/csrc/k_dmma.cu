@@ -117,10 +117,16 @@ __global__ void __launch_bounds__(128) dmma_gemm_kernel(const GemmView* __restri
       return advance_pair();
     };
 
+    // 8-row / 8-column groups of this warp's 32 x 32 sub-block inside the
+    // tile: DMMAs on groups wholly past the tile edge (zero-filled, never
+    // stored) are skipped, as are 4-k steps past the pair's k extent.
+    const int xr = max(0, min(4, (m - r0 - wm + 7) / 8));
+    const int yc = max(0, min(4, (n - c0 - wn + 7) / 8));
     bool have = advance_pair();
     int buf = 0;
     if (have) load(0);
     while (have) {
+      const int kv = min(BK, kk - kcur);   // valid k of the chunk in `buf`
       const bool more = next_chunk();
       if (more) load(buf ^ 1);
       if (more) cp_wait<1>(); else cp_wait<0>();
@@ -128,6 +134,7 @@ __global__ void __launch_bounds__(128) dmma_gemm_kernel(const GemmView* __restri
       const Stage& s = st[buf];
 #pragma unroll
       for (int k4 = 0; k4 < BK; k4 += 4) {
+        if (k4 >= kv) break;
         double af[4], bf[4];
 #pragma unroll
         for (int x = 0; x < 4; ++x) af[x] = s.a[wm + x * 8 + g][k4 + q];
@@ -136,7 +143,8 @@ __global__ void __launch_bounds__(128) dmma_gemm_kernel(const GemmView* __restri
 #pragma unroll
         for (int x = 0; x < 4; ++x)
 #pragma unroll
-          for (int y = 0; y < 4; ++y) dmma(acc[x][y], af[x], bf[y]);
+          for (int y = 0; y < 4; ++y)
+            if (x < xr && y < yc) dmma(acc[x][y], af[x], bf[y]);
       }
       __syncthreads();
       buf ^= 1;

@@ -1840,7 +1840,8 @@ tagpu_status ozaki_autotune(OzakiPlan* pl, int sm_count, cudaStream_t s, const c
     }
   }
   ozaki_enqueue(pl, sm_count, s);  // frames and bricks for the timing runs
-  const int shapes[][2] = {{4, 19}, {2, 38}, {8, 10}, {1, 76}, {19, 4}};
+  const int shapes[][2] = {{4, 19}, {2, 38}, {8, 10}, {1, 76}, {19, 4}, {6, 13}, {3, 25}, {12, 6}};
+  std::string all;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -1859,6 +1860,9 @@ tagpu_status ozaki_autotune(OzakiPlan* pl, int sm_count, cudaStream_t s, const c
       cudaEventElapsedTime(&ms, e0, e1);
       t = std::min(t, ms);
     }
+    char one[64];
+    snprintf(one, sizeof(one), " %dx%d:%.3f", sh[0], sh[1], t);
+    all += one;
     if (t < best) {
       best = t;
       bgr = sh[0];
@@ -1877,10 +1881,12 @@ tagpu_status ozaki_autotune(OzakiPlan* pl, int sm_count, cudaStream_t s, const c
   }
   if (log) {
     char buf[256];
-    snprintf(buf, sizeof(buf), "tuned %s: super-tile %dx%d, %.3f ms", key.c_str(), bgr, bgc,
-             best);
-    *log = buf;
+    snprintf(buf, sizeof(buf), "tuned %s: super-tile %dx%d, %.3f ms (ms per shape:", key.c_str(),
+             bgr, bgc, best);
+    *log = std::string(buf) + all + ")";
   }
+  if (const char* e = getenv("TAGPU_VERBOSE"))
+    if (atoi(e) > 0) fprintf(stderr, "tagpu: %s\n", log ? log->c_str() : all.c_str());
   return TAGPU_OK;
 }
 
