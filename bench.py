@@ -528,11 +528,14 @@ def run_serve(args, w, ta, wl, prec):
     th = threading.Thread(target=submitter)
     th.start()
     th.join()
-    results = []
-    for rid in ids:
+    results, failures = [], {}
+    for x, rid in enumerate(ids):
         if rid is not None:
             C, res = srv.wait(rid, 600000)
             results.append(res)
+            if res["status"] != 0:
+                key = f"{pool[picks[x]][5]}: status {res['status']}"
+                failures[key] = failures.get(key, 0) + 1
             del C
     wall = time.perf_counter() - t0
     st = srv.stats()
@@ -545,7 +548,8 @@ def run_serve(args, w, ta, wl, prec):
                        "150 GB admission budget", "precision": args.precision},
           {"latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"], "mean": st["mean_ms"]},
            "requests_per_s": len(results) / wall, "completed": st["completed"],
-           "rejected": st["rejected"] + rejected[0], "batches": st["batches"],
+           "rejected": st["rejected"] + rejected[0], "failed": st["failed"],
+           "failures": failures, "batches": st["batches"],
            "peak_admitted_bytes": st["peak_bytes"]})
 
 
