@@ -514,6 +514,7 @@ def run_serve(args, w, ta, wl, prec):
     picks = rng.integers(0, len(pool), args.requests)
     ids, rejected = [None] * args.requests, [0]
     t0 = time.perf_counter()
+    submitted = [0]
 
     def submitter():
         for x in range(args.requests):
@@ -525,18 +526,30 @@ def run_serve(args, w, ta, wl, prec):
                 ids[x] = srv.submit(c, 1.0, A, a, B, b)
             except ta.TAGPUError:
                 rejected[0] += 1
-    th = threading.Thread(target=submitter)
-    th.start()
-    th.join()
+            submitted[0] = x + 1
+
+    # the clients take their results as they complete (in submission order),
+    # so finished results do not pile up in HBM
     results, failures = [], {}
-    for x, rid in enumerate(ids):
-        if rid is not None:
-            C, res = srv.wait(rid, 600000)
+
+    def collector():
+        for x in range(args.requests):
+            while submitted[0] <= x:
+                time.sleep(0.0005)
+            if ids[x] is None:
+                continue
+            C, res = srv.wait(ids[x], 600000)
             results.append(res)
             if res["status"] != 0:
                 key = f"{pool[picks[x]][5]}: status {res['status']}"
                 failures[key] = failures.get(key, 0) + 1
             del C
+    th = threading.Thread(target=submitter)
+    tc = threading.Thread(target=collector)
+    th.start()
+    tc.start()
+    th.join()
+    tc.join()
     wall = time.perf_counter() - t0
     st = srv.stats()
     srv.stop()

@@ -103,3 +103,37 @@ def test_server_concurrent_submitters(ta, world):
         assert res["status"] == 0
         assert np.array_equal(C.download(), ref)
     srv.stop()
+
+
+def test_server_results_held_count_against_budget(ta, world):
+    """A finished result stays in HBM until its client takes it, so it keeps
+    its bytes of the admission budget until then (requests wait in the queue
+    rather than fail for memory while results pile up): with nothing taken,
+    the server's bytes in use after all requests finished are exactly the
+    results' bytes, and zero once the client has taken them."""
+    import time
+    h = uneven(1200, 64, 200, 9)
+    A, _ = gpu_operand(ta, world, [h, h], 5, 0, kind=0)
+    B, _ = gpu_operand(ta, world, [h, h], 5, 1, kind=0)
+    ref, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI)
+    res_bytes = ref.info().elements * 8
+    ref = ref.download()
+    srv = ta.Server(world, hbm_budget_bytes=1 << 30, max_batch=2)
+    ids = [srv.submit("i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI)
+           for _ in range(6)]
+    st = srv.stats()
+    for _ in range(6000):
+        st = srv.stats()
+        if st["completed"] + st["failed"] == 6:
+            break
+        time.sleep(0.01)
+    assert st["completed"] == 6 and st["failed"] == 0
+    assert st["bytes_in_use"] == 6 * res_bytes
+    for rid in ids:
+        C, res = srv.wait(rid, 60000)
+        assert res["status"] == 0
+        assert np.array_equal(C.download(), ref)
+        del C
+    st = srv.stats()
+    srv.stop()
+    assert st["bytes_in_use"] == 0

@@ -2374,6 +2374,7 @@ struct tagpu_server {
     tagpu_array *A = nullptr, *B = nullptr;
     tagpu_contract_opts opts{};
     size_t bound = 0;        // footprint reserved at admission
+    size_t held = 0;         // result bytes kept for the client until it takes them
     double t_submit = 0, t_admit = 0;
     bool done = false;
     tagpu_array* C = nullptr;
@@ -2467,7 +2468,11 @@ void tagpu_server::run() {
       }
       r->res.latency_ms = t - r->t_submit;
       r->plan.reset();
+      // the result stays in HBM until the client takes it: it keeps its
+      // bytes of the admission budget until then
+      r->held = r->C ? r->C->bytes : 0;
       in_use -= r->bound;
+      in_use += r->held;
       r->done = true;
       t_last = t;
     }
@@ -2493,6 +2498,23 @@ void tagpu_server::run() {
         } else {
           ++it;
         }
+      }
+      if (batch.empty() && inflight.empty()) {
+        if (stopping) {
+          // results nobody took hold the budget: the queue can never run
+          for (auto& r : queue) {
+            r->res.status = TAGPU_ERR_STATE;
+            r->res.latency_ms = now_ms() - r->t_submit;
+            r->done = true;
+            ++failed;
+          }
+          queue.clear();
+          done_cv.notify_all();
+          break;
+        }
+        // nothing fits until a client takes a result (or a request arrives)
+        cv.wait(lk);
+        continue;
       }
     }
     // plan the admitted requests while the previous batch is on the GPU
@@ -2628,6 +2650,9 @@ static tagpu_status server_take(tagpu_server* s, uint64_t id, tagpu_array** c,
     delete r->C;
   }
   r->C = nullptr;
+  s->in_use -= r->held;
+  r->held = 0;
+  s->cv.notify_all();   // the freed bytes may admit queued requests
   s->all.erase(it);
   return TAGPU_OK;
 }
