@@ -840,6 +840,7 @@ struct SplitJob {
   const int32_t* E;           // frames of the operand's fused rows
   int64_t rows_total, k_total;
   const int32_t* bricks;      // nbricks x 2 (row block, k block)
+  const int4* hdr;            // per brick: tile of its first / last row, of its first / last k
   int64_t nbricks;
   uint8_t* pack;              // brick i of the job at pack + i * S * ROWS * 64 bytes
   int64_t brick0;
@@ -866,7 +867,7 @@ __device__ __forceinline__ uint32_t stage_chunk(int r, int g) {
 // lanes along rows: both coalesced.  A brick over more than kTable tiles
 // (tiles of a few elements) looks tile offsets up in global memory.
 template <int S, int ROWS>
-__global__ void __launch_bounds__(256, ROWS == BM ? 3 : 5) split_kernel(const SplitJob* __restrict__ jobs, int njobs,
+__global__ void __launch_bounds__(256, ROWS == BM ? 4 : 5) split_kernel(const SplitJob* __restrict__ jobs, int njobs,
                                                     int64_t total) {
   constexpr int SLICE = ROWS * BK * 2;        // image bytes per slice
   constexpr int SPAD = 4 * (ROWS + 1) * 16;   // staged bytes per slice
@@ -878,20 +879,40 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 3 : 5) split_kernel(const Sp
   __shared__ int s_kt[BK], s_lk[BK], s_kk[BK];
   __shared__ int64_t s_off[kTable];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int64_t gbi = blockIdx.x; gbi < total; gbi += gridDim.x) {
+  // A brick's header (its job, index, block coordinates and tile ranges) is
+  // fetched one iteration ahead, so its loads overlap the previous brick.
+  struct Hdr {
+    int job;
+    int64_t bi;
+    int rb, kb;
+    int4 h;
+  };
+  auto fetch = [&](int64_t g) {
+    Hdr x;
     int lo = 0, hi = njobs;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
-      if (jobs[mid].brick0 <= gbi) lo = mid; else hi = mid;
+      if (jobs[mid].brick0 <= g) lo = mid; else hi = mid;
     }
-    const SplitJob& J = jobs[lo];
+    x.job = lo;
+    x.bi = g - jobs[lo].brick0;
+    x.rb = jobs[lo].bricks[2 * x.bi];
+    x.kb = jobs[lo].bricks[2 * x.bi + 1];
+    x.h = jobs[lo].hdr[x.bi];
+    return x;
+  };
+  Hdr cur{};
+  if (blockIdx.x < total) cur = fetch(blockIdx.x);
+  for (int64_t gbi = blockIdx.x; gbi < total; gbi += gridDim.x) {
+    Hdr nxt = cur;
+    if (gbi + gridDim.x < total) nxt = fetch(gbi + gridDim.x);
+    const SplitJob& J = jobs[cur.job];
     const OperandView& v = J.v;
     const int64_t rows_total = J.rows_total, k_total = J.k_total;
-    const int64_t bi = gbi - J.brick0;
-    const int64_t r0 = (int64_t)J.bricks[2 * bi] * ROWS, k0 = (int64_t)J.bricks[2 * bi + 1] * BK;
-    const int rt0 = J.row_tile[r0], kt0 = J.k_tile[k0];
-    const int nr = J.row_tile[min(rows_total, r0 + ROWS) - 1] - rt0 + 1;
-    const int nk = J.k_tile[min(k_total, k0 + BK) - 1] - kt0 + 1;
+    const int64_t bi = cur.bi;
+    const int64_t r0 = (int64_t)cur.rb * ROWS, k0 = (int64_t)cur.kb * BK;
+    const int rt0 = cur.h.x, kt0 = cur.h.z;
+    const int nr = cur.h.y - rt0 + 1, nk = cur.h.w - kt0 + 1;
     const bool staged = nr * nk <= kTable;
     for (int i = threadIdx.x; i < ROWS; i += blockDim.x) {
       const int64_t gr = r0 + i;
@@ -1024,6 +1045,7 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 3 : 5) split_kernel(const Sp
       *reinterpret_cast<uint4*>(dst + p * SLICE + brick_offset(r, 8 * g)) =
           *reinterpret_cast<const uint4*>(img + p * SPAD + stage_chunk<ROWS>(r, g));
     }
+    cur = nxt;
   }
 }
 
@@ -1060,6 +1082,19 @@ __global__ void brick_slot_kernel(const int64_t* __restrict__ flag,
   } else {
     slot[x] = -1;
   }
+}
+
+// Tile ranges of every brick of a list: the tiles of its first and last
+// row and of its first and last k (rows and k in fused GEMM order).
+__global__ void brick_hdr_kernel(const int32_t* __restrict__ list, int64_t n,
+                                 const int32_t* __restrict__ row_tile,
+                                 const int32_t* __restrict__ k_tile, int64_t rows_total,
+                                 int64_t k_total, int ROWS, int4* __restrict__ hdr) {
+  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n) return;
+  const int64_t r0 = (int64_t)list[2 * x] * ROWS, k0 = (int64_t)list[2 * x + 1] * BK;
+  hdr[x] = make_int4(row_tile[r0], row_tile[min(rows_total, r0 + ROWS) - 1], k_tile[k0],
+                     k_tile[min(k_total, k0 + BK) - 1]);
 }
 
 // Units of work are pairs of output blocks (rb, 2c) and (rb, 2c+1), run by
@@ -1190,6 +1225,7 @@ struct OzakiPlan {
   int32_t *row_tile = nullptr, *row_local = nullptr, *k_tile = nullptr, *k_local = nullptr,
           *col_tile = nullptr, *col_local = nullptr, *rstart = nullptr, *cstart = nullptr;
   int32_t *row_ext = nullptr, *k_ext = nullptr, *col_ext = nullptr;   // tile extent per index
+  int4 *hdrA = nullptr, *hdrB = nullptr;   // brick headers of listA / listB
   int4* blk_ab = nullptr;
   int32_t *EA = nullptr, *EB = nullptr, *brickA = nullptr, *brickB = nullptr, *listA = nullptr,
           *listB = nullptr, *blk = nullptr, *blk_kb = nullptr;
@@ -1546,6 +1582,18 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
     count_launch();
     cudaMemcpyAsync(&pl->nB, scan + nfb, 8, cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
+    if ((st = pl->alloc(&pl->hdrA, pl->nA, err)) || (st = pl->alloc(&pl->hdrB, pl->nB, err)))
+      return st;
+    if (pl->nA) {
+      brick_hdr_kernel<<<blocks_for(pl->nA, 256), 256, 0, s>>>(
+          pl->listA, pl->nA, pl->row_tile, pl->k_tile, pl->M_total, pl->K_total, BM, pl->hdrA);
+      count_launch();
+    }
+    if (pl->nB) {
+      brick_hdr_kernel<<<blocks_for(pl->nB, 256), 256, 0, s>>>(
+          pl->listB, pl->nB, pl->col_tile, pl->k_tile, pl->N_total, pl->K_total, BN, pl->hdrB);
+      count_launch();
+    }
     std::vector<int32_t> h(nfb), t(nfb);
     cudaMemcpyAsync(h.data(), slot_cb, nfb * 4, cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
@@ -1687,13 +1735,14 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   pl->h_frames[1] = FrameJob{pl->vb, pl->cstart, pl->chunk0_b, pl->EB, pl->frame_items_a};
   pl->h_split_b = SplitJob{pl->vb,      pl->col_tile, pl->col_local, pl->k_tile,
                            pl->k_local, pl->col_ext,  pl->k_ext,     pl->EB,
-                           pl->N_total, pl->K_total,  pl->listB,     pl->nB,
-                           pl->Bpack,   0};
+                           pl->N_total, pl->K_total,  pl->listB,     pl->hdrB,
+                           pl->nB,      pl->Bpack,    0};
   pl->h_split_a.clear();
   for (int c = 0; c < pl->nchunk; ++c)
     pl->h_split_a.push_back(SplitJob{pl->va, pl->row_tile, pl->row_local, pl->k_tile,
                                      pl->k_local, pl->row_ext, pl->k_ext, pl->EA, pl->M_total,
                                      pl->K_total, pl->listA + 2 * pl->chunk_slot[c],
+                                     pl->hdrA + pl->chunk_slot[c],
                                      pl->chunk_slot[c + 1] - pl->chunk_slot[c], pl->Apack, 0});
   {
     const std::vector<FrameJob> fj(pl->h_frames, pl->h_frames + 2);
