@@ -451,24 +451,25 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
     // per k step for S = 6 instead of 21 of N = 64, and far fewer operand
     // bytes read from shared memory per product.
     //
-    // A level that restarts at this stage (restart_mask) is zeroed by the
-    // product of slice 1 with slice t-1 alone (accumulate off) once the
-    // epilogue has read it; the slices p >= max restarting level touch no
-    // restarting level and are issued before the wait.  At the first stage
+    // Levels that restart at this stage (restart_mask) are zeroed, once the
+    // epilogue has read them, by the products of slice 1 with slices t-1
+    // alone (accumulate off), one MMA per run of adjacent restarting levels;
+    // the slices p >= max restarting level touch no restarting level and are
+    // issued before the wait.  At the first stage
     // of a block every level restarts; they are read from the top down, so
     // each level's zeroing product and the slice whose lowest level it is go
     // out as soon as that level is free.
-    auto mma_levels = [&](uint32_t sb, int p, int ks, int lo, int hi) {
+    auto mma_levels = [&](uint32_t sb, int p, int ks, int lo, int hi, uint32_t acc = 1u) {
       const uint32_t a = sb + (p - 1) * A_SLICE_BYTES + ks * 256;
       const uint32_t b0 = sb + S * A_SLICE_BYTES + (lo - p - 1) * B_SLICE_BYTES + ks * 256;
       const int n = (hi - lo + 1) * BN;
       const uint32_t d0 = tmem + (lo - 2) * BN;
       if (n <= 256) {
-        tc_mma(d0, make_desc(a), make_desc(b0), idesc_n(n), 1u);
+        tc_mma(d0, make_desc(a), make_desc(b0), idesc_n(n), acc);
       } else {
         const int h = n / 2;   // a multiple of 32: B rows start on 8-row groups
-        tc_mma(d0, make_desc(a), make_desc(b0), idesc_n(h), 1u);
-        tc_mma(d0 + h, make_desc(a), make_desc(b0 + (h / 8) * 512), idesc_n(h), 1u);
+        tc_mma(d0, make_desc(a), make_desc(b0), idesc_n(h), acc);
+        tc_mma(d0 + h, make_desc(a), make_desc(b0 + (h / 8) * 512), idesc_n(h), acc);
       }
     };
     auto mma_zero = [&](uint32_t sb, int t) {
@@ -551,9 +552,18 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
               }
           if (!ok) break;
           if (lane == 0) {
+            // each run of adjacent restarting levels is zeroed by one product
+            // of slice 1 (accumulate off)
+            int zlo = 0;
 #pragma unroll
-            for (int t = 2; t <= TOP; ++t)
-              if ((z >> t) & 1u) mma_zero(sbase, t);
+            for (int t = 2; t <= TOP + 1; ++t) {
+              const bool on = t <= TOP && ((z >> t) & 1u);
+              if (on && !zlo) zlo = t;
+              if (!on && zlo) {
+                mma_levels(sbase, 1, 0, zlo, t - 1, 0u);
+                zlo = 0;
+              }
+            }
             // slice 1 over the levels that do not restart, in runs
             int lo = 2;
 #pragma unroll
