@@ -117,7 +117,10 @@ tagpu_status tagpu_array_set_shape(tagpu_array* a, const float* norms,
 
 /* Host tiles: the nonzero tiles in tile-ordinal order, each row-major over
  * its own range, concatenated; n = total element count
- * (tagpu_array_info().elements). */
+ * (tagpu_array_info().elements).  Registered host memory (tagpu_host_alloc
+ * buffers, or memory the caller registered with CUDA) moves with a copy
+ * kernel over a coherent host link; other memory with cudaMemcpyAsync.
+ * Both calls return when the copy is complete. */
 tagpu_status tagpu_array_upload(tagpu_array* a, const double* tiles, int64_t n);
 tagpu_status tagpu_array_download(const tagpu_array* a, double* tiles, int64_t n);
 
@@ -132,10 +135,9 @@ tagpu_status tagpu_array_generate(tagpu_array* a, uint64_t seed, uint64_t stream
                                   int compute_shape, float threshold);
 
 /* Pinned host buffers for staging operands and results (no counterpart in
- * the reference, whose tiles live in host memory).  Copies between device
- * arrays and these buffers run at the host link's full rate every time; some
- * other pinned allocators on this platform slow down after other large
- * transfers.  Free with tagpu_host_free. */
+ * the reference, whose tiles live in host memory): anonymous mappings on
+ * base pages registered with CUDA (cudaHostAlloc memory where registration
+ * fails).  Free with tagpu_host_free. */
 tagpu_status tagpu_host_alloc(tagpu_ctx* ctx, size_t bytes, void** p);
 tagpu_status tagpu_host_free(tagpu_ctx* ctx, void* p);
 
