@@ -277,7 +277,7 @@ def run_reference(args):
     At, Bt = pack(A), pack(B)
     threads = os.cpu_count() or 1
     vals, desc = [], ""
-    per_step = max(2.0, min(20.0, 120.0 / max(1, args.steps + args.warmup)))
+    per_step = max(0.5, min(args.cpu_seconds, 20.0, 120.0 / max(1, args.steps + args.warmup)))
     for s in range(args.warmup + args.steps):
         v, desc, dt = cpu_sample(At, Bt, h, scale, per_step, threads, seed=s)
         if s >= args.warmup:
