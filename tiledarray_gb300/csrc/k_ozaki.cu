@@ -831,13 +831,32 @@ __device__ __forceinline__ void split_digits(double x, int frame, uint32_t (&h)[
     }
     fx = (bits >> 63) ? -(int64_t)q : (int64_t)q;
   }
+  // d = ((v + 128) & 255) - 128, v = (v - d) / 256 from the least
+  // significant digit.  |fx| <= 2^(8S-1): for S <= 3 all in 32 bits; else the
+  // low three digits come from the low 24 bits and their carry (0 or 1)
+  // joins the high part, which gives the same digits as the recurrence on
+  // the whole 64-bit value (each step only reads the low 8 bits, and the
+  // high part contributes none of them until it is reached).
+  auto digit = [](int& v) {
+    const int d = ((v + 128) & 255) - 128;
+    v = (v - d) >> 8;
+    return __float_as_uint((float)d) >> 16;
+  };
+  if constexpr (S <= 3) {
+    int v = (int)fx;
 #pragma unroll
-  for (int p = S - 1; p >= 1; --p) {
-    const int d = (int)(((fx + 128) & 255) - 128);
-    h[p] = __float_as_uint((float)d) >> 16;
-    fx = (fx - d) >> 8;
+    for (int p = S - 1; p >= 1; --p) h[p] = digit(v);
+    h[0] = __float_as_uint((float)v) >> 16;
+  } else {
+    int lo = (int)(fx & 0xFFFFFF);
+    int hi = (int)(fx >> 24);
+#pragma unroll
+    for (int p = S - 1; p >= S - 3; --p) h[p] = digit(lo);
+    hi += lo;
+#pragma unroll
+    for (int p = S - 4; p >= 1; --p) h[p] = digit(hi);
+    h[0] = __float_as_uint((float)hi) >> 16;
   }
-  h[0] = __float_as_uint((float)fx) >> 16;
 }
 
 // A split job: the bricks of one operand (or of one row chunk of it) of one
