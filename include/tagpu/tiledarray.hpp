@@ -203,6 +203,42 @@ class DistArray {
     world_->check(tagpu_array_get_norms(h(), n.data()));
     return n;
   }
+  // TiledArray::truncate (conversions/truncate.h:52-80): the shape rebuilt
+  // from the stored tiles' norms; threshold < 0 means the context default
+  void truncate(float threshold = -1.0f) {
+    world_->check(tagpu_array_truncate(h(), threshold));
+  }
+  // is_zero(ordinal) of the shape (a tile absent from storage)
+  bool is_zero(int64_t ordinal) const { return tile_offsets().at(ordinal) < 0; }
+  // DistArray::find(ordinal).get() of a nonzero tile, row-major over its range
+  std::vector<double> find(int64_t ordinal) const {
+    tagpu_array_info i{};
+    world_->check(tagpu_array_get_info(h(), &i));
+    if (ordinal < 0 || ordinal >= i.ntiles_total)
+      throw Exception(TAGPU_ERR_INVALID, "tile ordinal out of range");
+    int64_t vol = 1, o = ordinal;
+    for (int d = i.rank - 1; d >= 0; --d) {
+      std::vector<int64_t> hm(i.ntiles[d] + 1);
+      world_->check(tagpu_array_get_hashmarks(h(), d, hm.data()));
+      const int64_t x = o % i.ntiles[d];
+      o /= i.ntiles[d];
+      vol *= hm[x + 1] - hm[x];
+    }
+    std::vector<double> t(vol);
+    world_->check(tagpu_array_get_tile(h(), ordinal, t.data(), vol));
+    return t;
+  }
+  // archive I/O in DistArray::serialize order (single rank)
+  void save(const std::string& path) const {
+    world_->check(tagpu_array_save(h(), path.c_str()));
+  }
+  static DistArray load(World& w, const std::string& path) {
+    tagpu_array* a = nullptr;
+    w.check(tagpu_array_load(w.ctx(), path.c_str(), &a));
+    DistArray r;
+    r.reset(a, &w);
+    return r;
+  }
   // make_array with synthetic tiles generated on the device
   void fill_random(uint64_t seed, uint64_t stream, int kind = 0,
                    const std::vector<double>* tile_scale = nullptr, float threshold = -1.0f) {

@@ -22,6 +22,16 @@ def test_facade_compiles(tmp_path):
     assert os.path.exists(build_facade(tmp_path))
 
 
+def test_facade_services_compile(tmp_path):
+    """truncate, is_zero, find, save and load compile as a TiledArray user
+    would call them (compile only)."""
+    obj = str(tmp_path / "facade_api.o")
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-c",
+                    "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "facade_api.cpp"), "-o", obj], check=True)
+    assert os.path.exists(obj)
+
+
 @pytest.mark.gpu
 def test_facade_runs(tmp_path):
     exe = build_facade(tmp_path)
