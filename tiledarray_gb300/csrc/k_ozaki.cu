@@ -1213,6 +1213,22 @@ __global__ void slot_pairs_kernel(const int32_t* __restrict__ blk, const int64_t
   }
 }
 
+// Unit b's slot list rotated left by rot[b] (0 <= rot[b] < its length):
+// out[off[b] + j] = in[off[b] + (j + rot[b]) mod n].  One warp per unit.
+__global__ void rotate_units_kernel(const int4* __restrict__ in, const int64_t* __restrict__ off,
+                                    const int32_t* __restrict__ rot, int64_t nblk,
+                                    int4* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (b >= nblk) return;
+  const int64_t o = off[b], n = off[b + 1] - o, r = rot[b];
+  for (int64_t j = lane; j < n; j += 32) {
+    int64_t x = j + r;
+    if (x >= n) x -= n;
+    out[o + j] = in[o + x];
+  }
+}
+
 __global__ void flag_nonzero_kernel(const int64_t* __restrict__ counts, int64_t n,
                                     int64_t* __restrict__ flag) {
   const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1502,6 +1518,51 @@ tagpu_status ozaki_schedule(OzakiPlan* pl, int gr, int gc, std::string* err) {
 
 // Plan: index maps, brick maps, block lists, scratch.  Host reads back only
 // the counts that size the allocations.
+// Rotations of the units' k lists for TAGPU_KPHASE (see ozaki_plan).
+tagpu_status kphase_rotate(OzakiPlan* pl, std::string* err) {
+  cudaStream_t s = pl->s;
+  constexpr int kGr = 4, kGc = 19, kClusters = 76, kUnitCost = 3;
+  const auto& hb = pl->h_blk;
+  const auto& ho = pl->h_off;
+  std::vector<int32_t> kb(pl->nkb);
+  if (pl->nkb) {
+    cudaMemcpyAsync(kb.data(), pl->blk_kb, kb.size() * 4, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+  }
+  const int64_t nsc = ((pl->CB + 1) / 2 + kGc - 1) / kGc;
+  std::vector<std::pair<std::pair<int64_t, int64_t>, int64_t>> key(pl->nblk);
+  for (int64_t b = 0; b < pl->nblk; ++b) {
+    const int64_t rb = hb[2 * b], cp = hb[2 * b + 1];
+    key[b] = {{(rb / kGr) * nsc + cp / kGc, (cp % kGc) * kGr + rb % kGr}, b};
+  }
+  std::sort(key.begin(), key.end());
+  std::vector<int64_t> t(kClusters, 0);
+  std::vector<int32_t> rot(pl->nblk, 0);
+  for (int64_t i = 0; i < pl->nblk; ++i) {
+    const int64_t b = key[i].second, c = i % kClusters;
+    const int64_t o = ho[b], n = ho[b + 1] - o;
+    const int64_t k0 = t[c] % pl->KB;
+    int64_t r = 0;
+    while (r < n && kb[o + r] < k0) ++r;   // first k block at or after the phase
+    rot[b] = (int32_t)(r < n ? r : 0);
+    t[c] += n + kUnitCost;
+  }
+  int32_t* d_rot = nullptr;
+  int4* rotated = nullptr;
+  tagpu_status st;
+  if ((st = pl->upload(&d_rot, rot, err)) || (st = pl->alloc(&rotated, pl->nkb, err))) return st;
+  rotate_units_kernel<<<blocks_for(pl->nblk * 32, 256), 256, 0, s>>>(pl->blk_ab, pl->blk_off,
+                                                                     d_rot, pl->nblk, rotated);
+  count_launch();
+  pl->blk_ab = rotated;
+  const cudaError_t ce = cudaStreamSynchronize(s);
+  if (ce != cudaSuccess) {
+    *err = std::string("k-phase rotation: ") + cudaGetErrorString(ce);
+    return TAGPU_ERR_CUDA;
+  }
+  return TAGPU_OK;
+}
+
 tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
                         const int32_t* h_nsz, const int32_t* h_ksz, int slices,
                         OzakiPlan** out, std::string* err) {
@@ -1706,6 +1767,15 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
     cudaMemcpyAsync(pl->h_off.data(), pl->blk_off, pl->h_off.size() * 8, cudaMemcpyDeviceToHost,
                     s);
     cudaStreamSynchronize(s);
+  }
+  // Optional (TAGPU_KPHASE=1; not yet measured on the GPU): start every
+  // unit's k list at the k block its start time points to in the default
+  // schedule (76 clusters, 4 x 19 super-tiles, one time step per stage), so
+  // the clusters of a wave walk the same k blocks together and share them in
+  // L2.  The rotation depends on the unit alone, never on the tuned schedule
+  // or row chunking, so results stay identical across those.
+  if (const char* e = getenv("TAGPU_KPHASE")) {
+    if (atoi(e) > 0 && pl->nblk > 0 && (st = kphase_rotate(pl.get(), err))) return st;
   }
   if ((st = pl->alloc(&pl->blk_rng, 2 * pl->nblk, err))) return st;
   // operand slices (A: the largest chunk)
