@@ -594,17 +594,21 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    ws, rank, local = dist_env()
+    if ws > 1:
+        # The emulated GEMM loads shared A bricks with cluster-multicast bulk
+        # copies; it runs only in single-GPU processes.  The path keeps every
+        # contraction on one GPU and has no sharded form, so a multi-rank job
+        # has nothing to measure.
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "n_gpus": ws, "skipped":
+                              "single-GPU engine: the emulated GEMM uses cluster-multicast "
+                              "loads and runs only in 1-GPU processes; no multi-GPU path"}),
+                  flush=True)
+        return 0
     if args.workload != "blocksparse":
         return run_secondary(args)
-
-    ws, rank, local = dist_env()
-    dist = None
-    if ws > 1:
-        import torch
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-
+    local = 0
     import tiledarray_gb300 as ta
     from tiledarray_gb300 import build as tb
     tb.build()
@@ -625,14 +629,9 @@ def main():
                             slices=args.slices)
         return C, st
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
     for _ in range(args.warmup):
         C, st = step()
         del C
-    barrier()
     w.sync()
     clk = Clocks(local)
     ms_list, stats = [], None
@@ -643,15 +642,11 @@ def main():
         if _ != args.steps - 1:
             del C
     w.sync()
-    barrier()
     clocks = clk.stop()
     total_ms = sum(ms_list)
     flops = stats["flops"]
-    from tiledarray_gb300.replicas import aggregate
-    job_ms, job_flops, ws = aggregate(total_ms, flops * args.steps, dist,
-                                      f"cuda:{local}" if dist is not None else None)
-    ms_step = job_ms / args.steps
-    value = job_flops / (job_ms * 1e-3) / 1e12
+    ms_step = total_ms / args.steps
+    value = flops * args.steps / (total_ms * 1e-3) / 1e12
     lat = sorted(ms_list)
     p50 = float(np.percentile(lat, 50))
     p99 = float(np.percentile(lat, 99))
@@ -692,13 +687,13 @@ def main():
                       prec == ta.PRECISION_OZAKI else None,
                       "pairs": stats["pairs"], "flops_per_step": flops,
                       "nonzero_result_tiles": stats["nonzero_result_tiles"],
-                      "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"},
+                      "l2": "inputs larger than L2 (no flush)", "parallelism": "single GPU"},
            "latency_ms": {"p50": p50, "p99": p99},
            "phases_ms": {k: stats[k] for k in ("ms_shape", "ms_pairs", "ms_split", "ms_gemm")},
            "roofline": roof, "clocks": clocks,
            "gpu_launches": int(stats["kernel_launches"])}
     # error vs plain FP64 (DMMA) on the device, and the plain form's speed
-    if rank == 0 and not args.no_plain and prec == ta.PRECISION_OZAKI:
+    if not args.no_plain and prec == ta.PRECISION_OZAKI:
         Cp, stp = ta.contract(w, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_FP64)
         x, y = C.download(), Cp.download()
         err = float(np.linalg.norm(x - y) / np.linalg.norm(y))
@@ -713,7 +708,7 @@ def main():
         out["emulated_over_plain"] = value / out["plain_fp64"]["value"]
         del Cp, x, y
     # end to end through the public API with host buffers
-    if rank == 0 and not args.no_e2e:
+    if not args.no_e2e:
         # pinned host buffers from the library (tagpu_host_alloc)
         a_host = w.host_array(A.info().elements)
         b_host = w.host_array(B.info().elements)
@@ -787,12 +782,9 @@ def main():
             v, desc, dt = cpu_sample(A_t, B_t, h, scale, args.cpu_seconds, threads)
             out["cpu_baseline"] = {"value": v, "unit": "TFLOP/s", "cores": threads,
                                    "kind": "port", "sample": desc, "seconds": dt}
-    if rank == 0:
-        print(json.dumps(out), flush=True)
+    print(json.dumps(out), flush=True)
     del A, B, C
     w.close()
-    if dist is not None:
-        dist.destroy_process_group()
 
 
 if __name__ == "__main__":

@@ -64,3 +64,9 @@ def test_noalloc_rejects_oversize(world):
     assert st == 1
     assert b"1048576" in world.L.tagpu_last_error(world.h)
     assert ta.STATUS[st] == "invalid argument"
+    # M * N = 2^80 wraps to 0 in int64: the bound is checked per factor first
+    big = 1 << 40
+    st = world.L.tagpu_pair_list_noalloc(world.h, big, big, 1, dummy, 0.1, dummy, 0.1, dummy,
+                                         0.1, dummy, None, 0, ctypes.byref(n), None)
+    assert st == 1
+    assert b"1048576" in world.L.tagpu_last_error(world.h)

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <string>
 
 #include "internal.h"
 
@@ -69,15 +70,31 @@ extern "C" tagpu_status tagpu_pair_list_noalloc(tagpu_ctx* ctx, int64_t M, int64
   if (!ctx) return TAGPU_ERR_INVALID;
   if (M < 0 || N < 0 || K < 0 || !offsets)
     return set_last_error(ctx, TAGPU_ERR_INVALID, "pair_list_noalloc: bad arguments");
-  if (M * N > kNoAllocMaxTiles)
+  // M and N are bounded one at a time before their product is formed, so a
+  // huge pair cannot overflow int64 and slip past the limit.
+  if ((N > 0 && M > kNoAllocMaxTiles / N) || (M > 0 && N > kNoAllocMaxTiles / M))
     return set_last_error(ctx, TAGPU_ERR_INVALID,
                           "pair_list_noalloc: M*N result tiles above the fixed scratch of "
                           "1048576 tiles");
   if (M * N > 0 && (!cnorm || (K > 0 && (!lnorm || !rnorm))))
     return set_last_error(ctx, TAGPU_ERR_INVALID, "pair_list_noalloc: null input");
   const int dev = context_device(ctx);
-  if (dev < 0 || dev >= 128 || cudaSetDevice(dev) != cudaSuccess)
+  int prev_dev = -1;
+  if (cudaGetDevice(&prev_dev) != cudaSuccess) {
+    cudaGetLastError();
+    prev_dev = -1;
+  }
+  if (dev < 0 || dev >= 128 || cudaSetDevice(dev) != cudaSuccess) {
+    cudaGetLastError();
     return set_last_error(ctx, TAGPU_ERR_CUDA, "pair_list_noalloc: cannot select the device");
+  }
+  // the caller's current device is put back on every return below
+  struct RestoreDevice {
+    int d;
+    ~RestoreDevice() {
+      if (d >= 0) cudaSetDevice(d);
+    }
+  } restore{prev_dev};
   int64_t* counts = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -104,15 +121,25 @@ extern "C" tagpu_status tagpu_pair_list_noalloc(tagpu_ctx* ctx, int64_t M, int64
   int64_t np = 0;
   if (cudaMemcpyAsync(&np, offsets + MN, sizeof(np), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess) {
-    cudaGetLastError();
-    return TAGPU_ERR_CUDA;
+    const cudaError_t ce = cudaGetLastError();
+    return set_last_error(ctx, TAGPU_ERR_CUDA,
+                          (std::string("pair_list_noalloc: pair count: ") + cudaGetErrorString(ce)).c_str());
   }
   if (npairs) *npairs = np;
   if (kidx) {
     if (kidx_cap < np)
       return set_last_error(ctx, TAGPU_ERR_INVALID, "pair_list_noalloc: kidx capacity too small");
     launch_pair_emit(s, M, N, K, cnorm, c_thr, lnorm, l_thr, rnorm, r_thr, offsets, kidx);
-    if (cudaStreamSynchronize(s) != cudaSuccess) return TAGPU_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+      const cudaError_t ce = cudaGetLastError();
+      return set_last_error(ctx, TAGPU_ERR_CUDA,
+                            (std::string("pair_list_noalloc: pair emission: ") +
+                             cudaGetErrorString(ce)).c_str());
+    }
   }
-  return cudaGetLastError() == cudaSuccess ? TAGPU_OK : TAGPU_ERR_CUDA;
+  const cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess)
+    return set_last_error(ctx, TAGPU_ERR_CUDA,
+                          (std::string("pair_list_noalloc: ") + cudaGetErrorString(ce)).c_str());
+  return TAGPU_OK;
 }
