@@ -188,9 +188,11 @@ def dist_env():
     return ws, rank, local
 
 
-def cpu_sample(A_t, B_t, h, scale, seconds, threads, seed=0):
+def cpu_sample(A_t, B_t, h, scale, seconds, threads, seed=0, keep=False):
     """Oracle (vendor-BLAS dgemm per tile pair) on a bounded sample of result
-    tiles of the same contraction; returns (TFLOP/s, sample description)."""
+    tiles of the same contraction; returns (TFLOP/s, sample description,
+    seconds) and, with keep, the oracle's tiles (selected ordinals, their
+    offsets into the buffer, the buffer)."""
     import oracle as O
     fn = O.openblas_dgemm()
     thr = 1e-8
@@ -227,7 +229,7 @@ def cpu_sample(A_t, B_t, h, scale, seconds, threads, seed=0):
                               P(B_t["data"], O._f64p), P(B_t["offsets"], O._i64p), 0,
                               P(offs, O._i64p), P(kidx, O._i32p), 1.0, P(cbuf, O._f64p),
                               P(res_off, O._i64p), P(sel, O._i64p), len(sel), threads, fn)
-        return sel, time.perf_counter() - t0
+        return sel, time.perf_counter() - t0, res_off, cbuf
 
     # calibrate on a small sample, then size the timed sample to `seconds`
     def take(budget):
@@ -239,13 +241,45 @@ def cpu_sample(A_t, B_t, h, scale, seconds, threads, seed=0):
                 break
         return sel
     cal = take(threads * 2e9)
-    csel, cdt = run(cal)
+    csel, cdt, _, _ = run(cal)
     rate = tile_fl[csel].sum() / max(cdt, 1e-6)
-    sel, dt = run(take(rate * seconds))
+    sel, dt, res_off, cbuf = run(take(rate * seconds))
     fl = tile_fl[sel].sum()
     desc = (f"{len(sel)} of {len(cand)} nonzero result tiles ({fl / tile_fl.sum() * 100:.2f}% "
             f"of the flops), per-pair {'OpenBLAS' if fn else 'oracle-loop'} dgemm, {threads} threads")
+    if keep:
+        return fl / dt / 1e12, desc, dt, (sel, res_off, cbuf)
     return fl / dt / 1e12, desc, dt
+
+
+def errors_vs_oracle(packed, offsets, h, oracle_tiles):
+    """Relative Frobenius error of a GPU result (packed tiles, per-ordinal
+    offsets) against the oracle's tiles: over all checked tiles together,
+    the largest over single tiles, and the largest per band of |i - j|."""
+    sel, res_off, cbuf = oracle_tiles
+    nt = len(h) - 1
+    sizes = np.diff(np.asarray(h))
+    num = den = 0.0
+    worst = 0.0
+    band = {}
+    for t in sel:
+        i, j = int(t) // nt, int(t) % nt
+        m, n = int(sizes[i]), int(sizes[j])
+        ref = cbuf[res_off[t]:res_off[t] + m * n]
+        o = int(offsets[t])
+        got = packed[o:o + m * n] if o >= 0 else np.zeros(m * n)
+        d = float(np.dot(got - ref, got - ref))
+        r = float(np.dot(ref, ref))
+        num += d
+        den += r
+        if r > 0:
+            e = (d / r) ** 0.5
+            worst = max(worst, e)
+            b = abs(i - j) // 10 * 10
+            band[b] = max(band.get(b, 0.0), e)
+    return {"rel_err": (num / den) ** 0.5 if den > 0 else 0.0, "max_tile_rel_err": worst,
+            "tiles_checked": int(len(sel)),
+            "max_tile_rel_err_by_band": {f"{b}-{b + 9}": band[b] for b in sorted(band)}}
 
 
 def run_reference(args):
@@ -654,11 +688,19 @@ def main():
     pairs_per = SLICE_PAIRS.get(args.slices, 21) if prec == ta.PRECISION_OZAKI else 1
     gemm_ms = stats["ms_gemm"]
     if prec == ta.PRECISION_OZAKI:
-        achieved = flops * pairs_per / (gemm_ms * 1e-3) / 1e12
+        # the tensor work the GEMM issued: digit-slice MMAs over 128 x 64 x 32
+        # stage blocks (padding of partial blocks included), fewer than
+        # pairs_per per FP64 flop where digit shifts drop slice pairs
+        mma = stats["mma_flops"] or flops * pairs_per
+        achieved = mma / (gemm_ms * 1e-3) / 1e12
         roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                 "frac": achieved / bf16_peak, "traffic": None,
-                "kernel": "ozaki_gemm (bf16 digit-slice products, "
-                          f"{pairs_per} per FP64 product)", "peak_kind": f"{peak_kind} bf16 burst"}
+                "kernel": "ozaki_gemm (bf16 digit-slice MMAs issued; "
+                          f"{mma / flops:.2f} bf16 flops per FP64 flop, {pairs_per} without "
+                          "digit shifts)", "peak_kind": f"{peak_kind} bf16 burst",
+                "mma_flops_per_step": mma,
+                "fp64_equivalent": {"achieved": flops * pairs_per / (gemm_ms * 1e-3) / 1e12,
+                                    "note": f"{pairs_per} slice products per FP64 product"}}
         if args.n == 16384 and args.slices == 6 and args.seed == 0:
             tb = profiled_traffic("ozaki_gemm_blocksparse.md")
             if tb:
@@ -692,10 +734,14 @@ def main():
            "phases_ms": {k: stats[k] for k in ("ms_shape", "ms_pairs", "ms_split", "ms_gemm")},
            "roofline": roof, "clocks": clocks,
            "gpu_launches": int(stats["kernel_launches"])}
+    # results kept for the comparison with the oracle's tiles (CPU leg)
+    kept_results = {"emulated" if prec == ta.PRECISION_OZAKI else "plain":
+                    (C.download(), C.tile_offsets())}
     # error vs plain FP64 (DMMA) on the device, and the plain form's speed
     if not args.no_plain and prec == ta.PRECISION_OZAKI:
         Cp, stp = ta.contract(w, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_FP64)
         x, y = C.download(), Cp.download()
+        kept_results["plain"] = (y, Cp.tile_offsets())
         err = float(np.linalg.norm(x - y) / np.linalg.norm(y))
         dmma_peak, dfma_peak = w.fp64_rates()
         out["plain_fp64"] = {"value": flops / (stp["ms_total"] * 1e-3) / 1e12,
@@ -706,7 +752,11 @@ def main():
                              dmma_peak}
         out["rel_err_vs_plain_fp64"] = err
         out["emulated_over_plain"] = value / out["plain_fp64"]["value"]
-        del Cp, x, y
+        imma, hmma = w.mma_sync_rates()
+        out["mma_sync_rates"] = {"int8_tops": imma, "bf16_tflops": hmma,
+                                 "note": "warp-level mma.sync paths of this GPU (measured); "
+                                         "the emulated form runs on tcgen05 bf16"}
+        del Cp, x
     # end to end through the public API with host buffers
     if not args.no_e2e:
         # pinned host buffers from the library (tagpu_host_alloc)
@@ -779,11 +829,16 @@ def main():
             A_t = {"data": a_host, "offsets": A.tile_offsets(), "norms": A.norms()}
             B_t = {"data": b_host, "offsets": B.tile_offsets(), "norms": B.norms()}
             threads = os.cpu_count() or 1
-            v, desc, dt = cpu_sample(A_t, B_t, h, scale, args.cpu_seconds, threads)
+            v, desc, dt, otiles = cpu_sample(A_t, B_t, h, scale, args.cpu_seconds, threads,
+                                             keep=True)
             out["cpu_baseline"] = {"value": v, "unit": "TFLOP/s", "cores": threads,
                                    "kind": "port", "sample": desc, "seconds": dt}
+            # both GPU forms against the oracle's per-pair FP64 dgemm tiles
+            out["vs_oracle"] = {k: errors_vs_oracle(pk, po, h, otiles)
+                                for k, (pk, po) in kept_results.items()}
+            del otiles
     print(json.dumps(out), flush=True)
-    del A, B, C
+    del A, B, C, kept_results
     w.close()
 
 

@@ -93,6 +93,20 @@ tagpu_status tagpu_timer_stop(tagpu_ctx* ctx, double* ms);
  * and FMA, from short dependent-chain loops (~0.1 s).  No counterpart in the
  * reference; used as the plain form's roofline denominator. */
 tagpu_status tagpu_device_fp64_rates(tagpu_ctx* ctx, double* dmma_tflops, double* dfma_tflops);
+/* Measured rates of the warp-level tensor path (mma.sync) of the context's
+ * GPU: INT8 m16n8k32 (TOP/s) and bf16 m16n8k16 (TFLOP/s), ~0.3 s.  No
+ * counterpart in the reference; the evidence for the emulated form's choice
+ * of the tcgen05 bf16 path over INT8 (tcgen05 kind::i8 does not exist on
+ * sm_103a, leaving INT8 only on mma.sync). */
+tagpu_status tagpu_device_mma_sync_rates(tagpu_ctx* ctx, double* imma_tops, double* hmma_tflops);
+
+/* Bound of every pipeline wait inside the emulated GEMM (seconds, default
+ * 4).  A wait that runs out makes the kernel abort cleanly (in-flight copies
+ * and MMAs finish, tensor memory is released) and the call return
+ * TAGPU_ERR_TIMEOUT; the context stays usable.  Applies to contractions
+ * planned after the call (a batch keeps the bound it was captured with).
+ * No counterpart in the reference. */
+tagpu_status tagpu_set_wait_limit(tagpu_ctx* ctx, double seconds);
 
 /* Default screening threshold used for new result shapes; initial value is
  * FLT_EPSILON as in SparseShape<float>. */
@@ -151,6 +165,25 @@ tagpu_status tagpu_host_free(tagpu_ctx* ctx, void* p);
 tagpu_status tagpu_array_save(const tagpu_array* a, const char* path);
 tagpu_status tagpu_array_load(tagpu_ctx* ctx, const char* path, tagpu_array** a);
 
+/* The byte stream DistArray::serialize (dist_array.h:1583-1590) hands a
+ * MADNESS binary archive on one rank, for exchange with TiledArray programs:
+ * typeid hash of the array type, world size 1, rank 0, the TiledRange
+ * (tiled_range.h:392; tiled_range1.h:405; range.h:1143-1157), the shape
+ * (SparseShape: norm tensor, tile-extent vectors, zero count,
+ * sparse_shape.h:1918-1923; DenseShape: nothing), typeid hash of the pmap
+ * type, the tile count and every stored tile as a Tensor<double>
+ * (tensor/tensor.h:1389-1416).  The two hash codes belong to the C++
+ * implementation of the TiledArray build that reads or wrote the stream:
+ * serialize writes the values given, deserialize returns the values read.
+ * `sparse` says whether the stream holds a SparseShape (TSpArrayD) or a
+ * DenseShape (TArrayD); the stream does not record it.  Multi-rank streams
+ * are rejected (one rank's stream holds only that rank's tiles). */
+tagpu_status tagpu_array_serialize(const tagpu_array* a, const char* path,
+                                   uint64_t array_type_hash, uint64_t pmap_type_hash);
+tagpu_status tagpu_array_deserialize(tagpu_ctx* ctx, const char* path, int sparse,
+                                     tagpu_array** a, uint64_t* array_type_hash,
+                                     uint64_t* pmap_type_hash);
+
 /* TiledArray::truncate (conversions/truncate.h:52-80): the shape is rebuilt
  * from the Frobenius norms of the stored tiles (computed on the device in
  * storage order, as Tensor::norm), scaled by tile volume, with `threshold`
@@ -186,7 +219,7 @@ tagpu_status tagpu_array_get_hashmarks(const tagpu_array* a, int d,
 /* ---- contraction -------------------------------------------------------- */
 typedef struct tagpu_contract_opts {
   int precision;              /* tagpu_precision */
-  int slices;                 /* Ozaki slices per operand, 2..6, 0 = default (6) */
+  int slices;                 /* Ozaki slices per operand, 2..7, 0 = default (6) */
   float threshold;            /* result screening threshold, <0 = default */
   int autotune;               /* emulated form: time the GEMM schedules (block
                                  order, accumulation chunk) on first use of a
@@ -214,6 +247,10 @@ typedef struct tagpu_contract_stats {
   int64_t gemm_blocks;        /* output blocks the GEMM ran */
   int64_t gemm_launches;      /* GEMM-phase kernel launches */
   int64_t kernel_launches;    /* every kernel the call launched */
+  double mma_flops;           /* emulated form: bf16 flops of the digit-slice
+                                 MMAs issued (stages and slice pairs whose
+                                 products fall below the kept levels are
+                                 not issued) */
 } tagpu_contract_stats;
 
 /* c = alpha * A(a_idx) * B(b_idx) with index strings like "i,k".  *c is a new

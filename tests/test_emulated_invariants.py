@@ -39,22 +39,37 @@ def digits_32(fx, S):
             h[p], v = step(v)
         h[0] = v
         return h
-    lo, hi = to_i32(fx & 0xFFFFFF), to_i32(fx >> 24)
+    if S <= 6:
+        lo, hi = to_i32(fx & 0xFFFFFF), to_i32(fx >> 24)
+        for p in range(S - 1, S - 4, -1):
+            h[p], lo = step(lo)
+        hi += lo
+        for p in range(S - 4, 0, -1):
+            h[p], hi = step(hi)
+        h[0] = hi
+        return h
+    # S = 7 (|fx| <= 2^55): three 32-bit parts, the low two of 24 bits, each
+    # part's carry joining the next
+    lo, mid, top = to_i32(fx & 0xFFFFFF), to_i32((fx >> 24) & 0xFFFFFF), to_i32(fx >> 48)
     for p in range(S - 1, S - 4, -1):
         h[p], lo = step(lo)
-    hi += lo
-    for p in range(S - 4, 0, -1):
-        h[p], hi = step(hi)
-    h[0] = hi
+    mid += lo
+    for p in range(S - 4, S - 7, -1):
+        h[p], mid = step(mid)
+    top += mid
+    for p in range(S - 7, 0, -1):
+        h[p], top = step(top)
+    h[0] = top
     return h
 
 
-@pytest.mark.parametrize("S", [2, 3, 4, 5, 6])
+@pytest.mark.parametrize("S", [2, 3, 4, 5, 6, 7])
 def test_digit_split_forms_agree(S):
     lim = 1 << (8 * S - 1)     # |fixed point| <= 2^(8S-1)
     rng = random.Random(S)
     edges = [0, 1, -1, 127, 128, -128, -129, 255, 256, -256, lim, -lim, lim - 1, -lim + 1,
-             (1 << 24) - 1, 1 << 24, -(1 << 24), (1 << 24) + 128, -(1 << 24) - 128]
+             (1 << 24) - 1, 1 << 24, -(1 << 24), (1 << 24) + 128, -(1 << 24) - 128,
+             (1 << 48) - 1, 1 << 48, -(1 << 48), (1 << 48) + (1 << 24) - 128, -(1 << 48) - 129]
     values = [v for v in edges if abs(v) <= lim] + [rng.randint(-lim, lim) for _ in range(20000)]
     for fx in values:
         d64, d32 = digits_64(fx, S), digits_32(fx, S)

@@ -67,7 +67,8 @@ def test_ozaki_uniform_vs_oracle(oracle, ta, world, n, lo, hi, seed, decay):
     assert st["pairs"] == stp["pairs"]
 
 
-@pytest.mark.parametrize("slices,bound", [(3, 1e-5), (4, 1e-7), (5, 1e-9), (6, 1e-12)])
+@pytest.mark.parametrize("slices,bound", [(3, 1e-5), (4, 1e-7), (5, 1e-9), (6, 1e-12),
+                                          (7, 1e-14)])
 def test_ozaki_slices(oracle, ta, world, slices, bound):
     h = uneven(400, 40, 120, 9)
     A, _ = gpu_operand(ta, world, [h, h], 5, 0, kind=0)

@@ -72,7 +72,8 @@ class ContractStats(ctypes.Structure):
                 ("ms_total", ctypes.c_double), ("left_permtype", ctypes.c_int),
                 ("right_permtype", ctypes.c_int), ("precision", ctypes.c_int),
                 ("slices", ctypes.c_int), ("gemm_blocks", ctypes.c_int64),
-                ("gemm_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
+                ("gemm_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64),
+                ("mma_flops", ctypes.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -122,9 +123,11 @@ SIGNATURES = {
     "tagpu_sync": (ctypes.c_int, [_vp]),
     "tagpu_timer_start": (ctypes.c_int, [_vp]),
     "tagpu_device_fp64_rates": (ctypes.c_int, [_vp, _f64p, _f64p]),
+    "tagpu_device_mma_sync_rates": (ctypes.c_int, [_vp, _f64p, _f64p]),
     "tagpu_timer_stop": (ctypes.c_int, [_vp, _f64p]),
     "tagpu_threshold_get": (ctypes.c_float, [_vp]),
     "tagpu_threshold_set": (None, [_vp, ctypes.c_float]),
+    "tagpu_set_wait_limit": (ctypes.c_int, [_vp, ctypes.c_double]),
     "tagpu_array_create": (ctypes.c_int, [_vp, ctypes.c_int, _i64p,
                                           ctypes.POINTER(_i64p), ctypes.POINTER(_vp)]),
     "tagpu_array_destroy": (ctypes.c_int, [_vp]),
@@ -142,6 +145,12 @@ SIGNATURES = {
     "tagpu_host_alloc": (ctypes.c_int, [_vp, ctypes.c_size_t, ctypes.POINTER(_vp)]),
     "tagpu_host_free": (ctypes.c_int, [_vp, _vp]),
     "tagpu_array_load": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_vp)]),
+    "tagpu_array_serialize": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_uint64,
+                                             ctypes.c_uint64]),
+    "tagpu_array_deserialize": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int,
+                                               ctypes.POINTER(_vp),
+                                               ctypes.POINTER(ctypes.c_uint64),
+                                               ctypes.POINTER(ctypes.c_uint64)]),
     "tagpu_contract_accumulate": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, _vp,
                                                  ctypes.c_char_p, _vp, ctypes.c_char_p, _vp,
                                                  _vp]),
@@ -229,6 +238,16 @@ class World:
 
     def sync(self):
         self.check(self.L.tagpu_sync(self.h))
+
+    def set_wait_limit(self, seconds):
+        """Bound (seconds) of every pipeline wait in the emulated GEMM."""
+        self.check(self.L.tagpu_set_wait_limit(self.h, float(seconds)))
+
+    def mma_sync_rates(self):
+        """Measured (INT8 TOP/s, bf16 TFLOP/s) of the warp-level mma.sync path."""
+        a, b = ctypes.c_double(0), ctypes.c_double(0)
+        self.check(self.L.tagpu_device_mma_sync_rates(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def fp64_rates(self):
         """Measured (DMMA, DFMA) TFLOP/s of this GPU."""
@@ -506,8 +525,14 @@ class DistArray:
             int(compute_shape), np.float32(threshold)))
 
     def save(self, path):
-        """Archive of the array (DistArray::serialize order, single rank)."""
+        """The engine's own archive of the array (versioned, streamed)."""
         self.world.check(self.world.L.tagpu_array_save(self.h, os.fsencode(path)))
+
+    def serialize(self, path, array_type_hash=0, pmap_type_hash=0):
+        """The byte stream DistArray::serialize writes to a MADNESS binary
+        archive on one rank (the hash codes are the reading build's)."""
+        self.world.check(self.world.L.tagpu_array_serialize(
+            self.h, os.fsencode(path), int(array_type_hash), int(pmap_type_hash)))
 
     @staticmethod
     def load(world, path):
@@ -515,6 +540,17 @@ class DistArray:
         h = _vp()
         world.check(world.L.tagpu_array_load(world.h, os.fsencode(path), ctypes.byref(h)))
         return DistArray(world, _handle=h)
+
+    @staticmethod
+    def deserialize(world, path, sparse=True):
+        """An array read from a DistArray::serialize stream of one rank;
+        returns (array, array type hash, pmap type hash)."""
+        h = _vp()
+        th, ph = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        world.check(world.L.tagpu_array_deserialize(world.h, os.fsencode(path), int(sparse),
+                                                    ctypes.byref(h), ctypes.byref(th),
+                                                    ctypes.byref(ph)))
+        return DistArray(world, _handle=h), th.value, ph.value
 
     def truncate(self, threshold=-1.0):
         """TiledArray::truncate: shape from the stored tiles' norms, small tiles dropped."""

@@ -75,6 +75,9 @@ int64_t permute_items(const PermuteDesc& d, const int64_t* ext);
 // FP64 tensor (DMMA) and FMA rates measured with dependent-chain loops.
 tagpu_status measure_fp64_rates(cudaStream_t s, int sm_count, double* dmma_tflops,
                                 double* dfma_tflops);
+// INT8 (TOP/s) and bf16 (TFLOP/s) rates of the warp-level mma.sync path.
+tagpu_status measure_mma_sync_rates(cudaStream_t s, int sm_count, double* imma_tops,
+                                    double* hmma_tflops);
 
 // Generation of synthetic operands and sequential tile norms.
 struct GenDesc {
@@ -135,10 +138,11 @@ void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s);
 void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s);
 // One launch over the output blocks of several plans with the same slice
 // count: d_params holds their parameter blocks (ozaki_params), d_vstart the
-// prefix sums of their block counts; d_err receives a wait timeout.
+// prefix sums of their block counts; d_err receives a wait timeout (each
+// pipeline wait gives up after wait_ns).  Runs the stage-shift pass first.
 void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int nviews,
                               int64_t nblk, int slices, int* d_err, int sm_count,
-                              cudaStream_t s);
+                              unsigned long long wait_ns, cudaStream_t s);
 // Number of row chunks (1 unless the A digit bricks would not fit at once;
 // chunked plans are launched on their own, not grouped with others).
 int ozaki_chunks(const OzakiPlan* pl);
@@ -152,6 +156,10 @@ int ozaki_slices(const OzakiPlan* pl);
 int* ozaki_error_flag(OzakiPlan* pl);
 int ozaki_error(OzakiPlan* pl);   // synchronises; 0 = ok
 size_t ozaki_scratch_bytes(const OzakiPlan* pl);
+// Bound of the GEMM's pipeline waits for later runs of this plan.
+void ozaki_set_wait(OzakiPlan* pl, unsigned long long wait_ns);
+// bf16 flops of the digit-slice MMAs the last run issued; synchronises.
+double ozaki_mma_flops(OzakiPlan* pl);
 // Frames and digit splits of several plans of one digit count (none split in
 // row chunks) in one launch per step: the host builds the job tables (bytes
 // to upload as they are), the enqueue runs zeroing, frames, B and A splits.

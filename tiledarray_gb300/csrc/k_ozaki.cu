@@ -94,7 +94,14 @@ constexpr int A_SLICE_BYTES = BM * BK * 2;   // 8 KB
 constexpr int B_SLICE_BYTES = BN * BK * 2;   // 4 KB
 constexpr int EPI_WARPS = 8;
 constexpr int THREADS = 64 + EPI_WARPS * 32; // producer, MMA, 8 epilogue warps
-constexpr unsigned long long WAIT_NS = 4000000000ull;  // 4 s bound per wait
+// Bound of the waits that let in-flight copies and MMAs finish before a CTA
+// exits (they end within microseconds; the bound only keeps a broken launch
+// from spinning forever).  The pipeline waits take their bound from the
+// launch (wait_ns, host-settable, 4 s by default).
+constexpr unsigned long long WAIT_NS = 4000000000ull;
+// Brick shift of a brick with no nonzero element, and sum of shifts of a
+// stage without products (a column block past its last B brick).
+constexpr int32_t kNoShift = 1 << 20;
 
 // ---------------------------------------------------------------------------
 // PTX wrappers
@@ -127,15 +134,17 @@ __device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: false after WAIT_NS or when another role has aborted.
-__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile int* abort_s) {
+// Bounded wait: false after wait_ns or when another role has aborted.  The
+// timer is read after the first failed try and then every 64 tries.
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile int* abort_s,
+                                          unsigned long long wait_ns) {
   if (mbar_try(a, parity)) return true;
   const uint64_t t0 = globaltimer();
   for (uint32_t i = 0;; ++i) {
     if (mbar_try(a, parity)) return true;
-    if ((i & 63) == 63) {
+    if ((i & 63) == 0) {
       if (*abort_s) return false;
-      if (globaltimer() - t0 > WAIT_NS) return false;
+      if (globaltimer() - t0 > wait_ns) return false;
     }
   }
 }
@@ -292,8 +301,17 @@ struct OzParams {
   const int32_t* brickB;     // KBn x CB -> slot or -1
   const int32_t* blk;        // nblk x 2 (rb, cb), in scheduling order
   const int64_t* blk_rng;    // nblk x 2: [begin, end) of the block's k blocks in blk_kb
-  const int4* blk_ab;        // per k block of a unit: A slot, B slots of its two column
-                             // blocks (the zero brick where absent), unused
+  int4* blk_ab;              // per k block of a unit: A slot, B slots of its two column
+                             // blocks (the zero brick where absent), and the stage's
+                             // digit shifts (shift_kernel, every run): bits 0-7 the
+                             // shift of column block 0, 8-15 of column block 1, bit 16
+                             // set when neither CTA has a product (stage not loaded)
+  const int32_t* shiftA;     // per A brick slot: its deficit in bits, the least by which
+                             // its elements sit below their row frames (kNoShift: all zero)
+  const int32_t* shiftB;     // per B brick slot, likewise (slot of the zero brick: kNoShift)
+  int32_t* unitM;            // per unit and column block: level base M | extra levels << 28
+                             // (shift_kernel)
+  unsigned long long* products;  // digit-slice products issued (128 x 64 x 32 each)
   int64_t nblk;
   int KBn, CB;
   const int32_t* EA;         // M_total frames (biased exponent; E = EA - 1022)
@@ -332,17 +350,87 @@ __device__ __forceinline__ int find_view(const int64_t* __restrict__ vstart, int
   return lo;
 }
 
+// The MMAs of one stage whose levels are all written already, for shift SH
+// and last level L known at compile time: slice p feeds levels
+// p+1+SH .. p+SH+min(L-p-SH, S) with B slices 1.., one MMA (two above N =
+// 256) per slice and k step, every descriptor a constant offset from the
+// stage's.  Descriptor address fields count 16-byte units.
+template <int S, int SH, int L>
+__device__ __forceinline__ void stage_mmas(uint32_t tmem, uint64_t ad0, uint64_t bd0) {
+#pragma unroll
+  for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+    for (int p = 1; p <= S; ++p) {
+      const int nl = L - p - SH < S ? L - p - SH : S;
+      if (nl > 0) {
+        const uint64_t ad = ad0 + (uint64_t)(((p - 1) * A_SLICE_BYTES + ks * 256) >> 4);
+        const uint64_t bd = bd0 + (uint64_t)((ks * 256) >> 4);
+        const uint32_t d = tmem + (p - 1 + SH) * BN;
+        const int nn = nl * BN;
+        if (nn <= 256) {
+          tc_mma(d, ad, bd, idesc_n(nn), 1u);
+        } else {
+          const int h = nn / 2;
+          tc_mma(d, ad, bd, idesc_n(h), 1u);
+          tc_mma(d + h, ad, bd + (uint64_t)(((h / 8) * 512) >> 4), idesc_n(h), 1u);
+        }
+      }
+    }
+}
+// Selects the instance for a stage's shift s (0..S+1) and extra levels e.
+template <int S, int SH>
+__device__ __forceinline__ void stage_mmas_dispatch(int s, int e, uint32_t tmem, uint64_t ad0,
+                                                    uint64_t bd0) {
+  if constexpr (SH <= S + 1) {
+    if (s == SH) {
+      if (e == 0) {
+        stage_mmas<S, SH, S + 1>(tmem, ad0, bd0);
+      } else if (e == 1) {
+        if constexpr (S + 2 <= 9) stage_mmas<S, SH, S + 2>(tmem, ad0, bd0);
+      } else {
+        if constexpr (S + 3 <= 9) stage_mmas<S, SH, S + 3>(tmem, ad0, bd0);
+      }
+    } else {
+      stage_mmas_dispatch<S, SH + 1>(s, e, tmem, ad0, bd0);
+    }
+  }
+}
+
+// Digit shifts.  A brick's digits are cut relative to its rows' frames lowered
+// by 8 m bits: e, the brick's deficit, is the smallest number of bits by
+// which an element sits below its row frame, and m = floor(e / 8) whole
+// digits (split_kernel).  Operands that decay along k so keep all 8S-1 bits
+// in every brick instead of losing the bits between the brick and its row
+// maximum.  Product (p, q) of a stage whose bricks have mA and mB then has
+// weight 2^(2 - 8(p + q + mA + mB)) against the row and column frames.
+// An output block counts its levels from its base M = the smallest mA + mB
+// over its stages: product (p, q) of a stage with s = mA + mB - M lands on
+// level p + q + s.  Since mA + mB floors each deficit separately, the
+// block's largest contributions (deficit min(eA + eB) bits) may lie up to
+// u = min(eA + eB) - 8M < 15 bits below the base, so the block keeps
+// E = (u + 3) / 8 extra levels: pairs with p + q + s <= S + 1 + E are kept,
+// which puts the truncation at least 8S + 4 bits below the block's own
+// magnitude, as without shifts.  A stage with s >= S + E has no product
+// left; a stage that neither CTA of the cluster needs is not loaded at all.
+//
+// Lazy zeroing: a level restarts by being marked fresh; the first MMA that
+// writes a fresh level does so with accumulate off.  A level still fresh at a
+// drain got no product in its period, and the epilogue skips it.
 template <int S>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
     const OzParams* __restrict__ views, const int64_t* __restrict__ vstart, int nviews,
-    int64_t nblk_total, int* __restrict__ err) {
+    int64_t nblk_total, int* __restrict__ err, unsigned long long wait_ns) {
   constexpr int STAGES = Smem<S>::kStages;
   constexpr int STAGE_BYTES = Smem<S>::kStageBytes;
-  constexpr int TOP = S + 1;         // highest level (levels 2..S+1 are MMA targets)
+  // levels 2..TOP are MMA targets: S + 1 of them and up to two extra, as
+  // many as the 512 tensor-memory columns hold (one extra for S = 7)
+  constexpr int TOP = S + 3 < 9 ? S + 3 : 9;
+  static_assert((TOP - 1) * BN <= 512, "levels exceed tensor memory");
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES];
   __shared__ __align__(8) uint64_t bar_acc_full, bar_level[TOP + 1], bar_done;
   __shared__ uint32_t tmem_base_s;
+  __shared__ uint32_t fresh_ring[4];   // per drain: levels that got no product
   __shared__ volatile int abort_s;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -357,7 +445,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
       mbar_init(smem_u32(&bar_full[s]), 1);
       mbar_init(smem_u32(&bar_empty[s]), 2);   // both CTAs' MMAs have read the stage
     }
-    mbar_init(smem_u32(&bar_acc_full), 1);
+    // a drain is ready once the MMAs before it completed (commit) and the MMA
+    // warp has published the drain's fresh levels (arrive)
+    mbar_init(smem_u32(&bar_acc_full), 2);
     for (int t = 0; t <= TOP; ++t) mbar_init(smem_u32(&bar_level[t]), EPI_WARPS);  // per warp
     mbar_init(smem_u32(&bar_done), 1);
     abort_s = 0;
@@ -382,8 +472,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
-    // The whole warp loads 32 (A slot, B slot) pairs at a time; lane 0 waits
-    // for free stages and issues the two bulk copies of each.
+    // The whole warp loads 32 (A slot, B slot, shifts) entries at a time;
+    // lane 0 waits for free stages and issues the two bulk copies of each
+    // stage either CTA has products for.
     int stage = 0;
     uint32_t phase = 0;
     uint32_t issued_parity[STAGES];
@@ -402,8 +493,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
         for (int j = 0; j < cnt; ++j) {
           const int sa = __shfl_sync(0xffffffffu, mine.x, j);
           const int sb = __shfl_sync(0xffffffffu, rank ? mine.z : mine.y, j);
+          const int w = __shfl_sync(0xffffffffu, mine.w, j);
+          if ((w >> 16) & 1) continue;   // neither CTA has a product at this stage
           if (lane == 0) {
-            if (!mbar_wait(smem_u32(&bar_empty[stage]), phase ^ 1, &abort_s)) {
+            if (!mbar_wait(smem_u32(&bar_empty[stage]), phase ^ 1, &abort_s, wait_ns)) {
               fail(1);
               ok = false;
             } else {
@@ -435,7 +528,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
     // copies still in flight land before the CTA may exit
     if (lane == 0)
       for (int s = 0; s < STAGES; ++s)
-        if (issued[s] && !mbar_wait(smem_u32(&bar_full[s]), issued_parity[s], &abort_s)) {
+        if (issued[s] &&
+            !mbar_wait(smem_u32(&bar_full[s]), issued_parity[s], &abort_s, WAIT_NS)) {
           const uint64_t t0 = globaltimer();
           while (!mbar_try(smem_u32(&bar_full[s]), issued_parity[s]) &&
                  globaltimer() - t0 < WAIT_NS) {
@@ -445,25 +539,24 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
     // ------------------------------------------------------------ MMA issuer
     // Level t lives in tensor-memory columns [(t-2)*BN, (t-1)*BN) and the S
     // B slices of a stage are contiguous in the K-major image, so the
-    // products of A slice p with B slices for the adjacent levels lo..hi
-    // form ONE MMA of N = (hi-lo+1)*BN (two of half that width above 256).
-    // Slice p feeds the levels p+1..S+1: 8 MMAs of N >= 160, with one of 64,
-    // per k step for S = 6 instead of 21 of N = 64, and far fewer operand
-    // bytes read from shared memory per product.
+    // products of A slice p with B slices q = q0..q1 (levels p+q+s) form ONE
+    // MMA of N = (q1-q0+1)*BN (two of half that width above 256).  At shift
+    // s, with L = S+1+E the block's last level, slice p feeds levels
+    // p+1+s .. p+s+min(L-p-s, S): for s = 0, E = 0, 8 MMAs of N >= 160 and
+    // one of 64 per k step for S = 6.  Lane 0 issues; the other lanes join
+    // the waits.
     //
-    // Levels that restart at this stage (restart_mask) are zeroed, once the
-    // epilogue has read them, by the products of slice 1 with slices t-1
-    // alone (accumulate off), one MMA per run of adjacent restarting levels;
-    // the slices p >= max restarting level touch no restarting level and are
-    // issued before the wait.  At the first stage
-    // of a block every level restarts; they are read from the top down, so
-    // each level's zeroing product and the slice whose lowest level it is go
-    // out as soon as that level is free.
-    auto mma_levels = [&](uint32_t sb, int p, int ks, int lo, int hi, uint32_t acc = 1u) {
+    // At a stage where levels restart (restart_mask), the MMAs whose lowest
+    // level lies above every restarting level go first; then the warp waits
+    // until the epilogue has read the restarting levels, marks them fresh and
+    // issues the rest, slice 1 first (its range starts lowest).  An MMA over
+    // levels of which some are fresh is split into runs, fresh runs with
+    // accumulate off.
+    auto mma_run = [&](uint32_t sb, int p, int ks, int q0, int t0, int nlev, uint32_t acc) {
       const uint32_t a = sb + (p - 1) * A_SLICE_BYTES + ks * 256;
-      const uint32_t b0 = sb + S * A_SLICE_BYTES + (lo - p - 1) * B_SLICE_BYTES + ks * 256;
-      const int n = (hi - lo + 1) * BN;
-      const uint32_t d0 = tmem + (lo - 2) * BN;
+      const uint32_t b0 = sb + S * A_SLICE_BYTES + (q0 - 1) * B_SLICE_BYTES + ks * 256;
+      const int n = nlev * BN;
+      const uint32_t d0 = tmem + (t0 - 2) * BN;
       if (n <= 256) {
         tc_mma(d0, make_desc(a), make_desc(b0), idesc_n(n), acc);
       } else {
@@ -472,19 +565,35 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
         tc_mma(d0 + h, make_desc(a), make_desc(b0 + (h / 8) * 512), idesc_n(h), acc);
       }
     };
-    auto mma_zero = [&](uint32_t sb, int t) {
-      tc_mma(tmem + (t - 2) * BN, make_desc(sb),
-             make_desc(sb + S * A_SLICE_BYTES + (t - 2) * B_SLICE_BYTES), idesc_n(BN), 0u);
+    uint32_t fresh = 0;          // bit t: level t restarted and not written since (lane 0)
+    // Slice p at shift s up to level L, split by fresh runs (lane 0).
+    auto issue = [&](uint32_t sb, int p, int ks, int s, int L) {
+      const int lo = p + 1 + s, hi = p + s + min(L - p - s, S);
+      if (hi < lo) return;   // no level of this slice is kept (callers exclude it)
+      const uint32_t span = ((2u << hi) - 1u) & ~((1u << lo) - 1u);
+      if (!(fresh & span)) {
+        mma_run(sb, p, ks, 1, lo, hi - lo + 1, 1u);
+        return;
+      }
+      int t = lo;
+      while (t <= hi) {
+        const uint32_t f = (fresh >> t) & 1u;
+        int u = t;
+        while (u + 1 <= hi && ((fresh >> (u + 1)) & 1u) == f) ++u;
+        mma_run(sb, p, ks, t - p - s, t, u - t + 1, f ? 0u : 1u);
+        t = u + 1;
+      }
+      fresh &= ~span;
     };
     int stage = 0;
     uint32_t phase = 0;
     uint32_t level_parity = 0;   // bit t: parity of the next read of level t to wait for
-    uint32_t level_used = 0;     // bit t: level t has been written by this CTA
-    int64_t events = 0;          // acc_full commits
+    uint32_t level_used = 0;     // bit t: level t has been drained before
+    int64_t events = 0;          // drains published
     bool ok = true;
     auto wait_level = [&](int t) -> bool {
       if (level_used & (1u << t)) {
-        if (!mbar_wait(smem_u32(&bar_level[t]), (level_parity >> t) & 1u, &abort_s)) {
+        if (!mbar_wait(smem_u32(&bar_level[t]), (level_parity >> t) & 1u, &abort_s, wait_ns)) {
           fail(3);
           return false;
         }
@@ -498,101 +607,113 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
       const int vi = find_view(vstart, nviews, gb);
       const OzParams& P = views[vi];
       const int64_t b = gb - vstart[vi];
-      const int64_t n = P.blk_rng[2 * b + 1] - P.blk_rng[2 * b];
-      for (int64_t x = 0; x < n && ok; ++x) {
-        if (!mbar_wait(smem_u32(&bar_full[stage]), phase, &abort_s)) {
-          fail(2);
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        const uint32_t sbase = smem_u32(stage_base + stage * STAGE_BYTES);
-        const uint32_t z = restart_mask<TOP>(x);
-        if (x == 0) {
-#pragma unroll
-          for (int t = TOP; t >= 2; --t) {
-            if (!wait_level(t)) {
+      const int64_t x0 = P.blk_rng[2 * b];
+      const int64_t n = P.blk_rng[2 * b + 1] - x0;
+      const int L = S + 1 + (int)((uint32_t)P.unitM[2 * b + rank] >> 28);
+      const uint32_t* wsrc = reinterpret_cast<const uint32_t*>(P.blk_ab + x0) + 3;
+      uint32_t wnext = lane < n ? wsrc[4 * lane] : 0u;
+      for (int64_t xb = 0; xb < n && ok; xb += 32) {
+        const uint32_t wcur = wnext;   // the next 32 entries' shifts load meanwhile
+        if (xb + 32 + lane < n) wnext = wsrc[4 * (xb + 32 + lane)];
+        const int cnt = (int)(n - xb < 32 ? n - xb : 32);
+        for (int j = 0; j < cnt && ok; ++j) {
+          const int64_t x = xb + j;
+          const uint32_t w = __shfl_sync(0xffffffffu, wcur, j);
+          const int s = (int)((w >> (8 * rank)) & 0xffu);
+          const bool loaded = !((w >> 16) & 1u);
+          const bool has = loaded && s + 2 <= L;   // this CTA multiplies at this stage
+          const uint32_t z = restart_mask<TOP>(x);
+          uint32_t sbase = 0;
+          if (loaded) {
+            if (!mbar_wait(smem_u32(&bar_full[stage]), phase, &abort_s, wait_ns)) {
+              fail(2);
               ok = false;
               break;
             }
-            if (lane == 0) {
-              mma_zero(sbase, t);
-              if (t - 1 >= 2) mma_levels(sbase, t - 1, 0, t, TOP);
+            tc_fence_after();
+            sbase = smem_u32(stage_base + stage * STAGE_BYTES);
+          }
+          if (!z) {
+            if (lane == 0 && has) {
+              const uint32_t span = ((2u << L) - 1u) & ~((1u << (2 + s)) - 1u);
+              if (!(fresh & span)) {
+                // common case: every level of the stage is written already
+                stage_mmas_dispatch<S, 0>(s, L - S - 1, tmem, make_desc(sbase),
+                                          make_desc(sbase + S * A_SLICE_BYTES));
+              } else {
+#pragma unroll
+                for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+                  for (int p = 1; p <= S; ++p)
+                    if (p + 1 + s <= L) issue(sbase, p, ks, s, L);
+              }
             }
-            __syncwarp();
-          }
-          if (!ok) break;
-          if (lane == 0) {
+          } else if (x == 0) {
+            // a block's first stage: every level restarts.  Levels are read
+            // by the epilogue from the top down, so each slice goes out as
+            // soon as its lowest level is free.
 #pragma unroll
-            for (int p = 1; p <= S; ++p) mma_levels(sbase, p, 1, p + 1, TOP);
-          }
-        } else if (z == 0) {
-          if (lane == 0) {
-#pragma unroll
-            for (int ks = 0; ks < 2; ++ks)
-#pragma unroll
-              for (int p = 1; p <= S; ++p) mma_levels(sbase, p, ks, p + 1, TOP);
-          }
-        } else {
-          const int tmax = 31 - __clz(z);
-          if (lane == 0) {
-#pragma unroll
-            for (int ks = 0; ks < 2; ++ks)
-#pragma unroll
-              for (int p = 1; p <= S; ++p)
-                if (p >= tmax) mma_levels(sbase, p, ks, p + 1, TOP);
-          }
-          __syncwarp();
-#pragma unroll
-          for (int t = TOP; t >= 2; --t)
-            if ((z >> t) & 1u)
+            for (int t = TOP; t >= 2; --t) {
               if (!wait_level(t)) {
                 ok = false;
                 break;
               }
-          if (!ok) break;
-          if (lane == 0) {
-            // each run of adjacent restarting levels is zeroed by one product
-            // of slice 1 (accumulate off)
-            int zlo = 0;
-#pragma unroll
-            for (int t = 2; t <= TOP + 1; ++t) {
-              const bool on = t <= TOP && ((z >> t) & 1u);
-              if (on && !zlo) zlo = t;
-              if (!on && zlo) {
-                mma_levels(sbase, 1, 0, zlo, t - 1, 0u);
-                zlo = 0;
+              fresh |= 1u << t;
+              const int p = t - 1 - s;
+              if (lane == 0 && has && p >= 1 && p <= S && p + 1 + s <= L) {
+                issue(sbase, p, 0, s, L);
+                issue(sbase, p, 1, s, L);
               }
+              __syncwarp();
             }
-            // slice 1 over the levels that do not restart, in runs
-            int lo = 2;
+            if (!ok) break;
+          } else {
+            const int tmax = 31 - __clz(z);
+            if (lane == 0 && has) {
 #pragma unroll
-            for (int t = 2; t <= TOP + 1; ++t) {
-              if (t == TOP + 1 || ((z >> t) & 1u)) {
-                if (t > lo) mma_levels(sbase, 1, 0, lo, t - 1);
-                lo = t + 1;
-              }
+              for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+                for (int p = 1; p <= S; ++p)
+                  if (p + 1 + s > tmax && p + 1 + s <= L) issue(sbase, p, ks, s, L);
             }
+            __syncwarp();
 #pragma unroll
-            for (int p = 2; p <= S; ++p)
-              if (p < tmax) mma_levels(sbase, p, 0, p + 1, TOP);
+            for (int t = TOP; t >= 2; --t)
+              if ((z >> t) & 1u)
+                if (!wait_level(t)) {
+                  ok = false;
+                  break;
+                }
+            if (!ok) break;
+            fresh |= z;
+            if (lane == 0 && has) {
 #pragma unroll
-            for (int p = 1; p <= S; ++p)
-              if (p < tmax) mma_levels(sbase, p, 1, p + 1, TOP);
+              for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+                for (int p = 1; p <= S; ++p)
+                  if (p + 1 + s <= tmax && p + 1 + s <= L) issue(sbase, p, ks, s, L);
+            }
           }
-        }
-        __syncwarp();
-        // both CTAs write into this stage (the A halves): release it in both
-        if (lane == 0) tc_commit_mc(smem_u32(&bar_empty[stage]), (uint16_t)3);
-        __syncwarp();
-        if (++stage == STAGES) {
-          stage = 0;
-          phase ^= 1;
-        }
-        if (drain_mask<TOP>(x, n)) {
-          if (lane == 0) tc_commit(smem_u32(&bar_acc_full));
           __syncwarp();
-          ++events;
+          if (loaded) {
+            // both CTAs write into this stage (the A halves): release it in both
+            if (lane == 0) tc_commit_mc(smem_u32(&bar_empty[stage]), (uint16_t)3);
+            __syncwarp();
+            if (++stage == STAGES) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+          const uint32_t dm = drain_mask<TOP>(x, n);
+          if (dm) {
+            if (lane == 0) {
+              fresh_ring[events & 3] = fresh & dm;
+              tc_commit(smem_u32(&bar_acc_full));
+              mbar_arrive(smem_u32(&bar_acc_full));
+            }
+            __syncwarp();
+            ++events;
+          }
         }
       }
     }
@@ -608,10 +729,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
     // ------------------------------------------------------------ epilogue
     // Eight warps: warp % 4 selects the 32 tensor-memory lanes (rows) a warp
     // may access, (warp - 2) / 4 the half of the 64 columns it owns.  After
-    // each stage that ends a level's period (drain_mask), that level is read,
-    // released to the MMA warp at once, and folded into two int64
-    // accumulators per element: hi = L2*2^8 + L3 (unit of level 3) and
-    // lo = sum_{t>=4} L_t*2^(8(TOP-t)) (unit of level TOP).
+    // each stage that ends a level's period (drain_mask), that level is read
+    // (unless it got no product in the period), released to the MMA warp at
+    // once, and folded into two int64 accumulators per element: hi in units
+    // of level 5 takes the exact levels (L_t * 2^(8(5-t)), t <= 5; level 2's
+    // periods sum below 2^32 for K <= 2^18, so hi stays below 2^57) and lo in
+    // units of level TOP takes the whole-block levels (L_t * 2^(8(TOP-t)),
+    // t >= 6, each read once per block, below 2^59 together).
     const int quarter = warp & 3;
     const int half = (warp - 2) >> 2;
     const int rloc = quarter * 32 + lane;
@@ -630,16 +754,22 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
       for (int64_t x = 0; x < n; ++x) {
         const uint32_t dm = drain_mask<TOP>(x, n);
         if (!dm) continue;
-        if (!mbar_wait(smem_u32(&bar_acc_full), (uint32_t)(events & 1), &abort_s)) {
+        if (!mbar_wait(smem_u32(&bar_acc_full), (uint32_t)(events & 1), &abort_s, wait_ns)) {
           fail(4);
           ok = false;
           break;
         }
+        const uint32_t fm = fresh_ring[events & 3];
         ++events;
         tc_fence_after();
 #pragma unroll
         for (int t = TOP; t >= 2; --t) {
           if (!((dm >> t) & 1u)) continue;
+          if ((fm >> t) & 1u) {   // no product since the restart: the level is zero
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&bar_level[t]));
+            continue;
+          }
           float v0[16], v1[16];
           tmem_ld16(lane_addr + (t - 2) * BN, v0);
           tmem_ld16(lane_addr + (t - 2) * BN + 16, v1);
@@ -655,15 +785,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
               lo[j] += (int64_t)__float2ll_rn(v0[j]) << sh;
               lo[16 + j] += (int64_t)__float2ll_rn(v1[j]) << sh;
             }
-          } else if (t >= 4) {
-            const int sh = 8 * (TOP - t);
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              lo[j] += (int64_t)__float2int_rn(v0[j]) << sh;
-              lo[16 + j] += (int64_t)__float2int_rn(v1[j]) << sh;
-            }
           } else {
-            const int sh = 8 * (3 - t);
+            const int sh = 8 * (kExactTop - t);
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
               hi[j] += (int64_t)__float2int_rn(v0[j]) << sh;
@@ -673,11 +796,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
         }
       }
       if (!ok) break;
-      // recombination: C = alpha * 2^(E_A + E_B) * (hi * 2^(8(TOP-3)) + lo) * u_TOP,
+      // recombination: C = alpha * 2^(E_A + E_B - 8 M) * (hi * 2^(8(TOP-5)) + lo) * u_TOP,
       // exact integer to correctly rounded double, then one multiply by alpha
       const int64_t gr = (int64_t)rb * BM + rloc;
       if (gr < P.M_total) {
         const int ti = P.row_tile[gr], lr = P.row_local[gr], ea = P.EA[gr];
+        const int base = (int)((uint32_t)P.unitM[2 * b + rank] & 0x0FFFFFFFu);
         const bool unit_alpha = P.alpha == 1.0;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
@@ -686,8 +810,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
             const int tj = P.col_tile[gc];
             const int64_t off = P.coff[(int64_t)ti * P.Nt + tj];
             if (off >= 0) {
-              const double v = exact_to_double(hi[j], lo[j], 8 * (TOP - 3),
-                                               (2 - 8 * TOP) + (ea - 1022) + (P.EB[gc] - 1022));
+              const double v =
+                  exact_to_double(hi[j], lo[j], 8 * (TOP - kExactTop),
+                                  (2 - 8 * TOP) + (ea - 1022) + (P.EB[gc] - 1022) - 8 * base);
               const int64_t nn = P.nsz[tj];
               P.C[off + (P.hel * P.msz[ti] + lr) * nn + P.col_local[gc]] =
                   unit_alpha ? v : P.alpha * v;
@@ -707,6 +832,77 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
   tc_fence_after();
   if (warp == 1) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+  }
+}
+
+// Stage shifts of every unit (one warp per unit, all views of a launch).
+// From the bricks' deficits eA, eB (bits) and whole-digit shifts
+// mA = eA / 8, mB = eB / 8: each column block's base M = min(mA + mB) and
+// extra levels E = (min(eA + eB) - 8M + 3) / 8 (at most 2, and at most 1
+// for S = 7, whose levels 2..9 fill the tensor memory), packed as
+// unitM = M | E << 28; per stage s = mA + mB - M for each column block
+// (clipped to 255), bit 16 set when neither column block has a product
+// (s >= S + E).  Also counts the digit-slice products the GEMM will issue.
+__global__ void shift_kernel(const OzParams* __restrict__ views, const int64_t* __restrict__ vstart,
+                             int nviews, int64_t nblk_total, int S) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gb = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (gb >= nblk_total) return;
+  const int vi = find_view(vstart, nviews, gb);
+  const OzParams& P = views[vi];
+  const int64_t b = gb - vstart[vi];
+  const int64_t x0 = P.blk_rng[2 * b], x1 = P.blk_rng[2 * b + 1];
+  // deficits of the stage's A brick and its two B bricks (kNoShift: absent)
+  auto deficits = [&](int64_t x, int& a, int& b0, int& b1) {
+    const int4 e = P.blk_ab[x];
+    a = P.shiftA[e.x];
+    b0 = P.shiftB[e.y];
+    b1 = P.shiftB[e.z];
+  };
+  int M[2] = {kNoShift, kNoShift}, T[2] = {kNoShift, kNoShift};
+  for (int64_t x = x0 + lane; x < x1; x += 32) {
+    int a, bb[2];
+    deficits(x, a, bb[0], bb[1]);
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+      if (a < kNoShift && bb[c] < kNoShift) {
+        M[c] = min(M[c], (a >> 3) + (bb[c] >> 3));
+        T[c] = min(T[c], a + bb[c]);
+      }
+  }
+#pragma unroll
+  for (int c = 0; c < 2; ++c)
+    for (int o = 16; o > 0; o >>= 1) {
+      M[c] = min(M[c], __shfl_xor_sync(0xffffffffu, M[c], o));
+      T[c] = min(T[c], __shfl_xor_sync(0xffffffffu, T[c], o));
+    }
+  int E[2];
+#pragma unroll
+  const int emax = min(2, 9 - (S + 1));   // levels 2..9 fill the tensor memory
+  for (int c = 0; c < 2; ++c) E[c] = M[c] >= kNoShift ? 0 : min(emax, (T[c] - 8 * M[c] + 3) >> 3);
+  unsigned long long prod = 0;
+  for (int64_t x = x0 + lane; x < x1; x += 32) {
+    int a, bb[2];
+    deficits(x, a, bb[0], bb[1]);
+    int sh[2];
+    bool none = true;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const int L = S + 1 + E[c];
+      sh[c] = 255;
+      if (a < kNoShift && bb[c] < kNoShift) sh[c] = min(255, (a >> 3) + (bb[c] >> 3) - M[c]);
+      if (sh[c] + 2 <= L) {
+        none = false;
+        for (int p = 1; p <= S; ++p) prod += (unsigned long long)max(0, min(L - p - sh[c], S));
+      }
+    }
+    reinterpret_cast<int32_t*>(P.blk_ab + x)[3] = sh[0] | (sh[1] << 8) | ((none ? 1 : 0) << 16);
+  }
+  for (int o = 16; o > 0; o >>= 1) prod += __shfl_xor_sync(0xffffffffu, prod, o);
+  if (lane == 0) {
+    P.unitM[2 * b] = M[0] | (E[0] << 28);
+    P.unitM[2 * b + 1] = M[1] | (E[1] << 28);
+    if (prod) atomicAdd(P.products, prod);
   }
 }
 
@@ -820,7 +1016,7 @@ __device__ __forceinline__ void split_digits(double x, int frame, uint32_t (&h)[
       mant |= 1ull << 52;
     }
     const int E = frame - 1022;
-    const int sh = 1075 + E - (8 * S - 1) - bexp;   // >= 53 - (8S - 1) >= 0 for S <= 6
+    const int sh = 1075 + E - (8 * S - 1) - bexp;   // >= 53 - (8S - 1): negative only for S = 7
     uint64_t q;
     if (sh <= 0) {
       q = mant << (-sh);
@@ -847,7 +1043,7 @@ __device__ __forceinline__ void split_digits(double x, int frame, uint32_t (&h)[
 #pragma unroll
     for (int p = S - 1; p >= 1; --p) h[p] = digit(v);
     h[0] = __float_as_uint((float)v) >> 16;
-  } else {
+  } else if constexpr (S <= 6) {
     int lo = (int)(fx & 0xFFFFFF);
     int hi = (int)(fx >> 24);
 #pragma unroll
@@ -856,6 +1052,21 @@ __device__ __forceinline__ void split_digits(double x, int frame, uint32_t (&h)[
 #pragma unroll
     for (int p = S - 4; p >= 1; --p) h[p] = digit(hi);
     h[0] = __float_as_uint((float)hi) >> 16;
+  } else {
+    // |fx| <= 2^55: three digits from each of the two low 24-bit parts, each
+    // part's carry (0 or 1) joining the next, the rest from the top part
+    int lo = (int)(fx & 0xFFFFFF);
+    int mid = (int)((fx >> 24) & 0xFFFFFF);
+    int top = (int)(fx >> 48);
+#pragma unroll
+    for (int p = S - 1; p >= S - 3; --p) h[p] = digit(lo);
+    mid += lo;
+#pragma unroll
+    for (int p = S - 4; p >= S - 6; --p) h[p] = digit(mid);
+    top += mid;
+#pragma unroll
+    for (int p = S - 7; p >= 1; --p) h[p] = digit(top);
+    h[0] = __float_as_uint((float)top) >> 16;
   }
 }
 
@@ -872,6 +1083,7 @@ struct SplitJob {
   const int4* hdr;            // per brick: tile of its first / last row, of its first / last k
   int64_t nbricks;
   uint8_t* pack;              // brick i of the job at pack + i * S * ROWS * 64 bytes
+  int32_t* shift;             // brick i's deficit e in bits (kNoShift: all zero)
   int64_t brick0;
 };
 
@@ -907,6 +1119,7 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 4 : 5) split_kernel(const Sp
   __shared__ int s_rt[ROWS], s_lr[ROWS], s_fr[ROWS], s_m[ROWS];
   __shared__ int s_kt[BK], s_lk[BK], s_kk[BK];
   __shared__ int64_t s_off[kTable];
+  __shared__ int s_shift;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // A brick's header (its job, index, block coordinates and tile ranges) is
   // fetched one iteration ahead, so its loads overlap the previous brick.
@@ -943,6 +1156,9 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 4 : 5) split_kernel(const Sp
     const int rt0 = cur.h.x, kt0 = cur.h.z;
     const int nr = cur.h.y - rt0 + 1, nk = cur.h.w - kt0 + 1;
     const bool staged = nr * nk <= kTable;
+    // every reader of the previous brick's shift passed the barrier after
+    // its split before any thread gets here
+    if (threadIdx.x == 0) s_shift = kNoShift;
     for (int i = threadIdx.x; i < ROWS; i += blockDim.x) {
       const int64_t gr = r0 + i;
       if (gr < rows_total) {
@@ -1028,6 +1244,31 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 4 : 5) split_kernel(const Sp
       load_all(std::true_type{});
     else
       load_all(std::false_type{});
+    // Brick deficit e: the smallest number of bits by which a nonzero element
+    // sits below its row frame (subnormals count as exponent 1); the digits
+    // are cut against 2^(frame - 8m), m = floor(e / 8) whole digits.
+    {
+      int eloc = kNoShift;
+      auto see = [&](double val, int fr) {
+        if (val != 0.0 && fr > 0) eloc = min(eloc, fr - max(exp_field(val), 1));
+      };
+      if (!v.row_contig) {
+#pragma unroll
+        for (int i = 0; i < EPT; ++i) see(x[i], s_fr[warp + 8 * i]);
+      } else {
+#pragma unroll
+        for (int i = 0; i < EPT / 8; ++i) {
+          const int item = warp + 8 * i, r = (item >> 2) * 32 + lane;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) see(x[8 * i + j], s_fr[r]);
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) eloc = min(eloc, __shfl_xor_sync(0xffffffffu, eloc, o));
+      if (lane == 0 && eloc < kNoShift) atomicMin(&s_shift, eloc);
+    }
+    __syncthreads();
+    const int m = s_shift;
+    const int dfr = m < kNoShift ? 8 * (m >> 3) : 0;   // frame reduction of every row
     if (!v.row_contig) {
       const int k = lane;
       uint8_t* c0 = img + stage_chunk<ROWS>(0, k >> 3) + (k & 7) * 2;
@@ -1035,7 +1276,7 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 4 : 5) split_kernel(const Sp
       for (int i = 0; i < EPT; ++i) {
         const int r = warp + 8 * i;
         uint32_t h[S];
-        split_digits<S>(x[i], s_fr[r], h);
+        split_digits<S>(x[i], s_fr[r] - dfr, h);
 #pragma unroll
         for (int p = 0; p < S; ++p)
           *reinterpret_cast<uint16_t*>(c0 + r * 16 + p * SPAD) = (uint16_t)h[p];
@@ -1044,7 +1285,7 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 4 : 5) split_kernel(const Sp
 #pragma unroll
       for (int i = 0; i < EPT / 8; ++i) {
         const int item = warp + 8 * i, r = (item >> 2) * 32 + lane, g = item & 3;
-        const int fr = s_fr[r];
+        const int fr = s_fr[r] - dfr;
         uint32_t w[S][4];
 #pragma unroll
         for (int p = 0; p < S; ++p) w[p][0] = w[p][1] = w[p][2] = w[p][3] = 0;
@@ -1061,6 +1302,7 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 4 : 5) split_kernel(const Sp
           *reinterpret_cast<uint4*>(c + p * SPAD) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
       }
     }
+    if (threadIdx.x == 0) J.shift[bi] = m;
     __syncthreads();
     // Copy-out in image order (chunk c of a slice: row 8 (c / 32) + c % 8,
     // k group (c / 8) % 4).  The maps and staged offsets are not read again,
@@ -1286,6 +1528,9 @@ struct OzakiPlan {
   SplitJob* d_split_b = nullptr;
   SplitJob* d_split_a = nullptr;
   uint8_t *Apack = nullptr, *Bpack = nullptr;
+  int32_t *shiftA = nullptr, *shiftB = nullptr, *unitM = nullptr;   // digit shifts
+  unsigned long long* products = nullptr;  // digit-slice products issued per run
+  unsigned long long wait_ns = 4000000000ull;  // bound of the GEMM's pipeline waits
   int* err = nullptr;
   OzParams P{};
   OzParams* d_params = nullptr;   // P on the device (single-view launches)
@@ -1337,7 +1582,7 @@ constexpr int kMaxDevices = 128;
 
 template <int S>
 void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int64_t nblk,
-                   int* err, int sm_count, cudaStream_t st) {
+                   int* err, int sm_count, unsigned long long wait_ns, cudaStream_t st) {
   const size_t smem = Smem<S>::kBytes;
   // the shared-memory attribute and the co-resident cluster count are per
   // device
@@ -1370,7 +1615,11 @@ void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int
   // clusters of two CTAs, one unit (pair of output blocks) at a time each
   const int64_t grid = 2 * std::min<int64_t>(nblk, clusters[dev]);
   if (grid > 0) {
-    ozaki_gemm_kernel<S><<<(unsigned)grid, THREADS, smem, st>>>(views, vstart, nviews, nblk, err);
+    // stage shifts from the digit bricks just split, then the GEMM
+    shift_kernel<<<blocks_for(nblk * 32, 256), 256, 0, st>>>(views, vstart, nviews, nblk, S);
+    count_launch();
+    ozaki_gemm_kernel<S><<<(unsigned)grid, THREADS, smem, st>>>(views, vstart, nviews, nblk, err,
+                                                                wait_ns);
     count_launch();
   }
 }
@@ -1417,6 +1666,7 @@ void launch_split(int S, const SplitJob* d_jobs, int njobs, int64_t total, bool 
     case 3: launch_split_t<3>(d_jobs, njobs, total, a_side, sm_count, st); break;
     case 4: launch_split_t<4>(d_jobs, njobs, total, a_side, sm_count, st); break;
     case 5: launch_split_t<5>(d_jobs, njobs, total, a_side, sm_count, st); break;
+    case 7: launch_split_t<7>(d_jobs, njobs, total, a_side, sm_count, st); break;
     default: launch_split_t<6>(d_jobs, njobs, total, a_side, sm_count, st); break;
   }
 }
@@ -1498,6 +1748,7 @@ tagpu_status ozaki_schedule(OzakiPlan* pl, int gr, int gc, std::string* err) {
       cp[c].blk_rng = pl->P.blk_rng + 2 * pl->chunk_blk[c];
       cp[c].nblk = pl->chunk_blk[c + 1] - pl->chunk_blk[c];
       cp[c].a_slot_base = pl->chunk_slot[c];
+      cp[c].unitM = pl->P.unitM + 2 * pl->chunk_blk[c];
       cv[2 * c] = 0;
       cv[2 * c + 1] = cp[c].nblk;
     }
@@ -1566,8 +1817,8 @@ tagpu_status kphase_rotate(OzakiPlan* pl, std::string* err) {
 tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
                         const int32_t* h_nsz, const int32_t* h_ksz, int slices,
                         OzakiPlan** out, std::string* err) {
-  if (slices < 2 || slices > 6) {
-    *err = "emulated form supports 2..6 slices";
+  if (slices < 2 || slices > 7) {
+    *err = "emulated form supports 2..7 slices";
     return TAGPU_ERR_INVALID;
   }
   auto pl = std::make_unique<OzakiPlan>();
@@ -1785,9 +2036,14 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   if ((st = pl->alloc(&pl->Apack, a_brick * max_slots, err)) ||
       (st = pl->alloc(&pl->Bpack, b_brick * (pl->nB + 1), err)))
     return st;
+  if ((st = pl->alloc(&pl->shiftA, pl->nA, err)) ||
+      (st = pl->alloc(&pl->shiftB, pl->nB + 1, err)) ||
+      (st = pl->alloc(&pl->unitM, 2 * pl->nblk, err)) || (st = pl->alloc(&pl->products, 1, err)))
+    return st;
   // brick nB: all digits zero, read by a unit's column block where it has no
-  // B brick of its own
+  // B brick of its own; its shift marks it empty (0x3F3F3F3F >= kNoShift)
   cudaMemsetAsync(pl->Bpack + b_brick * pl->nB, 0, b_brick, s);
+  cudaMemsetAsync(pl->shiftB + pl->nB, 0x3F, sizeof(int32_t), s);
   cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) {
     *err = std::string("ozaki planning: ") + cudaGetErrorString(ce);
@@ -1821,6 +2077,10 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   P.N_total = pl->N_total;
   P.err = pl->err;
   P.a_slot_base = 0;
+  P.shiftA = pl->shiftA;
+  P.shiftB = pl->shiftB;
+  P.unitM = pl->unitM;
+  P.products = pl->products;
   if (pl->nchunk > 1 && ((st = pl->alloc(&pl->d_chunk_params, pl->nchunk, err)) ||
                          (st = pl->alloc(&pl->d_chunk_vstart, 2 * pl->nchunk, err))))
     return st;
@@ -1835,14 +2095,15 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   pl->h_split_b = SplitJob{pl->vb,      pl->col_tile, pl->col_local, pl->k_tile,
                            pl->k_local, pl->col_ext,  pl->k_ext,     pl->EB,
                            pl->N_total, pl->K_total,  pl->listB,     pl->hdrB,
-                           pl->nB,      pl->Bpack,    0};
+                           pl->nB,      pl->Bpack,    pl->shiftB,    0};
   pl->h_split_a.clear();
   for (int c = 0; c < pl->nchunk; ++c)
     pl->h_split_a.push_back(SplitJob{pl->va, pl->row_tile, pl->row_local, pl->k_tile,
                                      pl->k_local, pl->row_ext, pl->k_ext, pl->EA, pl->M_total,
                                      pl->K_total, pl->listA + 2 * pl->chunk_slot[c],
                                      pl->hdrA + pl->chunk_slot[c],
-                                     pl->chunk_slot[c + 1] - pl->chunk_slot[c], pl->Apack, 0});
+                                     pl->chunk_slot[c + 1] - pl->chunk_slot[c], pl->Apack,
+                                     pl->shiftA + pl->chunk_slot[c], 0});
   {
     const std::vector<FrameJob> fj(pl->h_frames, pl->h_frames + 2);
     const std::vector<SplitJob> sb(1, pl->h_split_b);
@@ -1859,6 +2120,7 @@ void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s) {
   cudaMemsetAsync(pl->EA, 0, pl->M_total * 4, s);
   cudaMemsetAsync(pl->EB, 0, pl->N_total * 4, s);
   cudaMemsetAsync(pl->err, 0, 4, s);
+  cudaMemsetAsync(pl->products, 0, sizeof(unsigned long long), s);
   launch_frames(pl->d_frames, 2, pl->frame_items_a + pl->frame_items_b, s);
   launch_split(pl->S, pl->d_split_b, 1, pl->nB, false, sm_count, s);
   // chunked plans split A chunk by chunk inside ozaki_enqueue_gemm
@@ -1867,27 +2129,29 @@ void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s) {
 
 void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int nviews,
                               int64_t nblk, int slices, int* d_err, int sm_count,
-                              cudaStream_t s) {
+                              unsigned long long wait_ns, cudaStream_t s) {
   const OzParams* v = static_cast<const OzParams*>(d_params);
   switch (slices) {
-    case 2: launch_gemm_t<2>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
-    case 3: launch_gemm_t<3>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
-    case 4: launch_gemm_t<4>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
-    case 5: launch_gemm_t<5>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
-    default: launch_gemm_t<6>(v, d_vstart, nviews, nblk, d_err, sm_count, s); break;
+    case 2: launch_gemm_t<2>(v, d_vstart, nviews, nblk, d_err, sm_count, wait_ns, s); break;
+    case 3: launch_gemm_t<3>(v, d_vstart, nviews, nblk, d_err, sm_count, wait_ns, s); break;
+    case 4: launch_gemm_t<4>(v, d_vstart, nviews, nblk, d_err, sm_count, wait_ns, s); break;
+    case 5: launch_gemm_t<5>(v, d_vstart, nviews, nblk, d_err, sm_count, wait_ns, s); break;
+    case 7: launch_gemm_t<7>(v, d_vstart, nviews, nblk, d_err, sm_count, wait_ns, s); break;
+    default: launch_gemm_t<6>(v, d_vstart, nviews, nblk, d_err, sm_count, wait_ns, s); break;
   }
 }
 
 void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s) {
   if (pl->nchunk == 1) {
     ozaki_enqueue_gemm_views(pl->d_params, pl->d_vstart, 1, pl->nblk, pl->S, pl->err, sm_count,
-                             s);
+                             pl->wait_ns, s);
     return;
   }
   for (int c = 0; c < pl->nchunk; ++c) {
     launch_split(pl->S, pl->d_split_a + c, 1, pl->h_split_a[c].nbricks, true, sm_count, s);
     ozaki_enqueue_gemm_views(pl->d_chunk_params + c, pl->d_chunk_vstart + 2 * c, 1,
-                             pl->chunk_blk[c + 1] - pl->chunk_blk[c], pl->S, pl->err, sm_count, s);
+                             pl->chunk_blk[c + 1] - pl->chunk_blk[c], pl->S, pl->err, sm_count,
+                             pl->wait_ns, s);
   }
 }
 
@@ -1914,7 +2178,8 @@ void ozaki_group_tables(OzakiPlan* const* pls, int n, std::vector<uint8_t>* zero
     append_bytes(zero_jobs, ZeroJob{pl->EA, pl->M_total});
     append_bytes(zero_jobs, ZeroJob{pl->EB, pl->N_total});
     append_bytes(zero_jobs, ZeroJob{pl->err, 1});
-    d->nzero += 3;
+    append_bytes(zero_jobs, ZeroJob{reinterpret_cast<int32_t*>(pl->products), 2});
+    d->nzero += 4;
     for (int x = 0; x < 2; ++x) {
       FrameJob f = pl->h_frames[x];
       f.item0 = d->frame_items;
@@ -2051,6 +2316,16 @@ int ozaki_error(OzakiPlan* pl) {
 }
 
 size_t ozaki_scratch_bytes(const OzakiPlan* pl) { return pl->bytes; }
+void ozaki_set_wait(OzakiPlan* pl, unsigned long long wait_ns) { pl->wait_ns = wait_ns; }
+
+// bf16 flops of the digit-slice MMAs the last run issued (128 x 64 x 32
+// multiply-adds per slice product); synchronises.
+double ozaki_mma_flops(OzakiPlan* pl) {
+  unsigned long long n = 0;
+  cudaMemcpyAsync(&n, pl->products, sizeof(n), cudaMemcpyDeviceToHost, pl->s);
+  cudaStreamSynchronize(pl->s);
+  return (double)n * 2.0 * BM * BN * BK;
+}
 int64_t ozaki_units(const OzakiPlan* pl) { return pl->nblk; }
 void ozaki_destroy(OzakiPlan* pl) { delete pl; }
 

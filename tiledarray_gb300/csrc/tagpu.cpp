@@ -51,6 +51,8 @@ struct tagpu_ctx {
   tagpu_contract_stats last{};
   std::recursive_mutex mu;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
+  // bound of every pipeline wait in the emulated GEMM (tagpu_set_wait_limit)
+  unsigned long long wait_ns = 4000000000ull;
 };
 
 struct tagpu_array {
@@ -560,9 +562,28 @@ tagpu_status tagpu_device_fp64_rates(tagpu_ctx* ctx, double* dmma_tflops, double
   return TAGPU_OK;
 }
 
+tagpu_status tagpu_device_mma_sync_rates(tagpu_ctx* ctx, double* imma_tops, double* hmma_tflops) {
+  if (!ctx || !imma_tops || !hmma_tflops) return TAGPU_ERR_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  tagpu_status st = measure_mma_sync_rates(ctx->stream, ctx->sm_count, imma_tops, hmma_tflops);
+  if (st) return fail(ctx, st, "mma.sync rate measurement failed");
+  return TAGPU_OK;
+}
+
 float tagpu_threshold_get(const tagpu_ctx* ctx) { return ctx ? ctx->threshold : 0.0f; }
 void tagpu_threshold_set(tagpu_ctx* ctx, float t) {
   if (ctx) ctx->threshold = t;
+}
+
+tagpu_status tagpu_set_wait_limit(tagpu_ctx* ctx, double seconds) {
+  if (!ctx) return TAGPU_ERR_INVALID;
+  if (!(seconds > 0.0) || seconds > 3600.0)
+    return fail(ctx, TAGPU_ERR_INVALID, "wait limit must lie in (0, 3600] seconds");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  const double ns = seconds * 1e9;
+  ctx->wait_ns = ns < 1.0 ? 1ull : (unsigned long long)ns;
+  return TAGPU_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -1127,6 +1148,267 @@ tagpu_status tagpu_array_load(tagpu_ctx* ctx, const char* path, tagpu_array** ou
       CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     }
   }
+  *out_a = a.release();
+  return TAGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Archives in DistArray::serialize field order (one rank)
+// ---------------------------------------------------------------------------
+// The stream a MADNESS binary archive receives from DistArray::serialize
+// (dist_array.h:1583-1590) for one rank: every scalar is its raw
+// little-endian bytes, arrays written through archive::wrap carry no length,
+// vectors carry a size_t count first.
+//   u64 typeid(DistArray).hash_code, i32 world size, i32 world rank,
+//   TiledRange  (tiled_range.h:392):  Range tiles, Range elements,
+//               u64 modes, per mode TiledRange1 (tiled_range1.h:405):
+//               Range1 tiles, Range1 elements, u64 ntiles, Range1 per tile
+//   shape       SparseShape (sparse_shape.h:1918-1923): Tensor<float> of the
+//               scaled norms, per mode ValArray<float> of tile extents
+//               (u64 size + floats, val_array.h:454-457), u64 zero count;
+//               DenseShape writes nothing (dense_shape.h:390)
+//   u64 typeid(pmap).hash_code, i64 tile count,
+//   per stored tile Tensor<double> (tensor/tensor.h:1389-1416):
+//               u8 empty, Range, u64 nbatch, f64 data[volume * nbatch]
+// Range (range.h:1143-1157): u32 rank, i64 lobound[r], upbound[r],
+// extent[r], stride[r] (row-major), i64 offset = sum lobound * stride,
+// u64 volume.  Range1 (range1.h:195-204): i64 first, i64 second.
+// The two hash codes are values of the writer's C++ implementation; they are
+// passed through, never interpreted.
+namespace {
+struct SerialRange {
+  std::vector<int64_t> lo, up;
+};
+bool put_range(File& f, const std::vector<int64_t>& lo, const std::vector<int64_t>& up) {
+  const uint32_t r = (uint32_t)lo.size();
+  bool ok = f.put<uint32_t>(r);
+  std::vector<int64_t> ext(r), stride(r);
+  int64_t vol = 1, off = 0;
+  for (int d = (int)r - 1; d >= 0; --d) {
+    ext[d] = up[d] - lo[d];
+    stride[d] = vol;
+    off += lo[d] * stride[d];
+    vol *= ext[d];
+  }
+  for (auto* v : {&lo, &up, (const std::vector<int64_t>*)&ext,
+                  (const std::vector<int64_t>*)&stride})
+    for (int64_t x : *v) ok = ok && f.put<int64_t>(x);
+  return ok && f.put<int64_t>(off) && f.put<uint64_t>((uint64_t)vol);
+}
+// Reads a Range and checks that its derived fields agree with its bounds.
+bool get_range(File& f, SerialRange* r, uint32_t max_rank = 8) {
+  uint32_t rank = 0;
+  if (!f.get(rank) || rank > max_rank) return false;
+  std::vector<int64_t> v(4 * (size_t)rank);
+  for (auto& x : v)
+    if (!f.get(x)) return false;
+  int64_t off = 0;
+  uint64_t vol = 0;
+  if (!f.get(off) || !f.get(vol)) return false;
+  r->lo.assign(v.begin(), v.begin() + rank);
+  r->up.assign(v.begin() + rank, v.begin() + 2 * rank);
+  int64_t evol = 1, eoff = 0;
+  for (int d = (int)rank - 1; d >= 0; --d) {
+    const int64_t ext = r->up[d] - r->lo[d];
+    if (ext < 0 || v[2 * rank + d] != ext || v[3 * rank + d] != evol) return false;
+    eoff += r->lo[d] * evol;
+    evol *= ext;
+  }
+  return eoff == off && (uint64_t)evol == vol;
+}
+}  // namespace
+
+tagpu_status tagpu_array_serialize(const tagpu_array* a, const char* path,
+                                   uint64_t array_type_hash, uint64_t pmap_type_hash) {
+  if (!a || !path) return TAGPU_ERR_INVALID;
+  tagpu_ctx* ctx = a->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  File out(path, "wb");
+  if (!out.f) return fail(ctx, TAGPU_ERR_INVALID, "serialize: cannot open %s", path);
+  PinnedStage stage;
+  if (!stage.p) return fail(ctx, TAGPU_ERR_NOMEM, "serialize: no pinned staging buffer");
+  const int r = a->rank;
+  bool ok = out.put<uint64_t>(array_type_hash) && out.put<int32_t>(1) && out.put<int32_t>(0);
+  // TiledRange: tile range, element range, the modes' TiledRange1
+  std::vector<int64_t> z(r, 0), nt(r), elo(r), eup(r);
+  for (int d = 0; d < r; ++d) {
+    nt[d] = a->nt[d];
+    elo[d] = a->hm[d].front();
+    eup[d] = a->hm[d].back();
+  }
+  ok = ok && put_range(out, z, nt) && put_range(out, elo, eup) && out.put<uint64_t>((uint64_t)r);
+  for (int d = 0; d < r && ok; ++d) {
+    ok = out.put<int64_t>(0) && out.put<int64_t>(a->nt[d]) && out.put<int64_t>(elo[d]) &&
+         out.put<int64_t>(eup[d]) && out.put<uint64_t>((uint64_t)a->nt[d]);
+    for (int64_t i = 0; i < a->nt[d] && ok; ++i)
+      ok = out.put<int64_t>(a->hm[d][i]) && out.put<int64_t>(a->hm[d][i + 1]);
+  }
+  const int64_t n = a->ntiles();
+  if (!a->dense) {
+    // SparseShape: the norm tensor over the tile range (nbatch 1), the tile
+    // extents of every mode as floats, the zero-tile count
+    ok = ok && out.put<uint8_t>(n == 0 ? 1 : 0);
+    if (n > 0) {
+      ok = ok && put_range(out, z, nt) && out.put<uint64_t>(1) &&
+           fwrite(a->norms.data(), 4, (size_t)n, out.f) == (size_t)n;
+    }
+    for (int d = 0; d < r && ok; ++d) {
+      ok = out.put<uint64_t>((uint64_t)a->nt[d]);
+      for (int64_t i = 0; i < a->nt[d] && ok; ++i)
+        ok = out.put<float>((float)(a->hm[d][i + 1] - a->hm[d][i]));
+    }
+    ok = ok && out.put<uint64_t>((uint64_t)a->zero_count);
+  }
+  int64_t count = 0;
+  for (int64_t t = 0; t < n; ++t) count += a->off[t] >= 0;
+  ok = ok && out.put<uint64_t>(pmap_type_hash) && out.put<int64_t>(count);
+  int64_t idx[8];
+  std::vector<int64_t> lo(r), up(r);
+  for (int64_t t = 0; t < n && ok; ++t) {
+    if (a->off[t] < 0) continue;
+    a->tile_index(t, idx);
+    for (int d = 0; d < r; ++d) {
+      lo[d] = a->hm[d][idx[d]];
+      up[d] = a->hm[d][idx[d] + 1];
+    }
+    ok = out.put<uint8_t>(0) && put_range(out, lo, up) && out.put<uint64_t>(1);
+    const size_t bytes = (size_t)a->tile_volume(t) * sizeof(double);
+    for (size_t x = 0; x < bytes && ok; x += kStage) {
+      const size_t m = std::min(kStage, bytes - x);
+      CUDA_TRY(ctx, cudaMemcpyAsync(stage.p, (const uint8_t*)(a->data + a->off[t]) + x, m,
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+      CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      ok = fwrite(stage.p, 1, m, out.f) == m;
+    }
+  }
+  if (!ok) return fail(ctx, TAGPU_ERR_INVALID, "serialize: write to %s failed", path);
+  return TAGPU_OK;
+}
+
+tagpu_status tagpu_array_deserialize(tagpu_ctx* ctx, const char* path, int sparse,
+                                     tagpu_array** out_a, uint64_t* array_type_hash,
+                                     uint64_t* pmap_type_hash) {
+  if (!ctx || !path || !out_a) return TAGPU_ERR_INVALID;
+  *out_a = nullptr;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  File in(path, "rb");
+  if (!in.f) return fail(ctx, TAGPU_ERR_INVALID, "deserialize: cannot open %s", path);
+  auto bad = [&](const char* what) {
+    return fail(ctx, TAGPU_ERR_INVALID, "deserialize: %s: %s", path, what);
+  };
+  uint64_t th = 0, ph = 0;
+  int32_t wsize = 0, wrank = 0;
+  if (!in.get(th) || !in.get(wsize) || !in.get(wrank)) return bad("truncated header");
+  if (wsize != 1 || wrank != 0)
+    return bad("archive of a multi-rank world (one rank's tiles only); this engine is one rank");
+  SerialRange tr, er;
+  uint64_t modes = 0;
+  if (!get_range(in, &tr) || !get_range(in, &er) || !in.get(modes) || modes != tr.lo.size())
+    return bad("bad TiledRange");
+  const int r = (int)modes;
+  std::vector<std::vector<int64_t>> hm(r);
+  for (int d = 0; d < r; ++d) {
+    int64_t t0, t1, e0, e1;
+    uint64_t cnt = 0;
+    if (!in.get(t0) || !in.get(t1) || !in.get(e0) || !in.get(e1) || !in.get(cnt))
+      return bad("bad TiledRange1");
+    if (t0 != tr.lo[d] || t1 != tr.up[d] || e0 != er.lo[d] || e1 != er.up[d] ||
+        (int64_t)cnt != t1 - t0 || cnt > (uint64_t(1) << 32))
+      return bad("TiledRange1 disagrees with the TiledRange");
+    hm[d].reserve(cnt + 1);
+    for (uint64_t i = 0; i < cnt; ++i) {
+      int64_t f = 0, s = 0;
+      if (!in.get(f) || !in.get(s) || s < f) return bad("bad tile range");
+      if (i == 0) {
+        if (f != e0) return bad("first tile does not start the element range");
+        hm[d].push_back(f);
+      } else if (f != hm[d].back()) {
+        return bad("tiles of a mode leave gaps");
+      }
+      hm[d].push_back(s);
+    }
+    if (cnt == 0) hm[d].push_back(e0);
+    if (hm[d].back() != e1) return bad("tiles do not end the element range");
+  }
+  std::unique_ptr<tagpu_array> a(new_array(ctx, hm));
+  const int64_t n = a->ntiles();
+  if (sparse) {
+    uint8_t empty = 1;
+    if (!in.get(empty)) return bad("truncated shape");
+    a->dense = false;
+    a->norms.assign((size_t)n, 0.0f);
+    if (!empty) {
+      SerialRange nr;
+      uint64_t nb = 0;
+      if (!get_range(in, &nr) || !in.get(nb) || nb != 1 || nr.lo != std::vector<int64_t>(r, 0) ||
+          nr.up != tr.up)
+        return bad("norm tensor does not span the tile range");
+      if (fread(a->norms.data(), 4, (size_t)n, in.f) != (size_t)n) return bad("truncated norms");
+    }
+    for (int d = 0; d < r; ++d) {
+      uint64_t sz = 0;
+      if (!in.get(sz) || (int64_t)sz != a->nt[d]) return bad("bad size vector");
+      for (uint64_t i = 0; i < sz; ++i) {
+        float x = 0;
+        if (!in.get(x) || x != (float)(hm[d][i + 1] - hm[d][i]))
+          return bad("size vector disagrees with the tiling");
+      }
+    }
+    uint64_t zc = 0;
+    if (!in.get(zc)) return bad("truncated shape");
+    int64_t zeros = 0;
+    for (float x : a->norms) zeros += x == 0.0f;
+    if ((int64_t)zc != zeros) return bad("zero-tile count disagrees with the norms");
+    a->zero_count = zeros;
+    // The writer's threshold is process-wide and not stored; every tile with
+    // a nonzero norm was kept by it, so the array's threshold is the context
+    // default lowered, if need be, to the smallest nonzero norm.
+    float thr = ctx->threshold;
+    for (float x : a->norms)
+      if (x > 0.0f && x < thr) thr = x;
+    a->threshold = thr;
+  }
+  int64_t count = -1;
+  if (!in.get(ph) || !in.get(count)) return bad("truncated");
+  pack_offsets(a.get());
+  tagpu_status st = ensure_storage(a.get());
+  if (st) return st;
+  int64_t expect = 0;
+  for (int64_t t = 0; t < n; ++t) expect += a->off[t] >= 0;
+  if (count != expect) return bad("stored tiles do not match the shape");
+  PinnedStage stage;
+  if (!stage.p) return fail(ctx, TAGPU_ERR_NOMEM, "deserialize: no pinned staging buffer");
+  std::vector<char> seen((size_t)n, 0);
+  for (int64_t c = 0; c < count; ++c) {
+    uint8_t empty = 1;
+    SerialRange tr1;
+    uint64_t nb = 0;
+    if (!in.get(empty) || empty || !get_range(in, &tr1) || !in.get(nb) || nb != 1 ||
+        (int)tr1.lo.size() != r)
+      return bad("bad tile header");
+    // the tile's ordinal from its lower bounds
+    int64_t t = 0;
+    for (int d = 0; d < r; ++d) {
+      const auto it = std::lower_bound(hm[d].begin(), hm[d].end() - 1, tr1.lo[d]);
+      if (it == hm[d].end() - 1 || *it != tr1.lo[d] || *(it + 1) != tr1.up[d])
+        return bad("tile range is not a tile of the TiledRange");
+      t = t * a->nt[d] + (it - hm[d].begin());
+    }
+    if (a->off[t] < 0 || seen[t]) return bad("tile absent from the shape or repeated");
+    seen[t] = 1;
+    const size_t bytes = (size_t)a->tile_volume(t) * sizeof(double);
+    for (size_t x = 0; x < bytes; x += kStage) {
+      const size_t m = std::min(kStage, bytes - x);
+      if (fread(stage.p, 1, m, in.f) != m) return bad("truncated tile data");
+      CUDA_TRY(ctx, cudaMemcpyAsync((uint8_t*)(a->data + a->off[t]) + x, stage.p, m,
+                                    cudaMemcpyHostToDevice, ctx->stream));
+      CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+  }
+  if (array_type_hash) *array_type_hash = th;
+  if (pmap_type_hash) *pmap_type_hash = ph;
   *out_a = a.release();
   return TAGPU_OK;
 }
@@ -1716,8 +1998,8 @@ tagpu_status plan_all(Contraction& c, const char* c_idx, double alpha, tagpu_arr
   const float cthr = opts && opts->threshold >= 0 ? opts->threshold : ctx->threshold;
   if (c.precision != TAGPU_PRECISION_FP64 && c.precision != TAGPU_PRECISION_OZAKI)
     return fail(ctx, TAGPU_ERR_INVALID, "unknown precision %d", c.precision);
-  if (c.precision == TAGPU_PRECISION_OZAKI && (c.slices < 2 || c.slices > 6))
-    return fail(ctx, TAGPU_ERR_INVALID, "slices must be 2..6");
+  if (c.precision == TAGPU_PRECISION_OZAKI && (c.slices < 2 || c.slices > 7))
+    return fail(ctx, TAGPU_ERR_INVALID, "slices must be 2..7");
   tagpu_status e;
   std::string err;
   if ((e = plan_contraction(c, c_idx, alpha, A, a_idx, B, b_idx, cthr))) return e;
@@ -1738,6 +2020,7 @@ tagpu_status plan_all(Contraction& c, const char* c_idx, double alpha, tagpu_arr
       e = ozaki_plan(ctx->stream, v, c.msz.data(), c.nsz.data(), c.ksz.data(), c.slices, &pl,
                      &err);
       if (e) return fail(ctx, e, "%s", err.c_str());
+      ozaki_set_wait(pl, ctx->wait_ns);
       c.ozs.push_back(pl);
       const size_t b = ozaki_scratch_bytes(pl);
       c.oz_bytes += b;
@@ -1921,7 +2204,7 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, Launch
       if (stream != ctx->stream) CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     }
     ozaki_enqueue_gemm_views(lb.ozp[S].p, lb.ozv[S].as<int64_t>(), (int)g.size(), lb.oz_nblk[S],
-                             S, ozaki_error_flag(g[0]), ctx->sm_count, stream);
+                             S, ozaki_error_flag(g[0]), ctx->sm_count, ctx->wait_ns, stream);
   }
   if (!items.empty()) {
     launch_dmma_gemm(stream, d_views.as<GemmView>(), d_items.as<WorkItem>(),
@@ -1985,6 +2268,7 @@ tagpu_status contract_impl(tagpu_ctx* ctx, const char* c_idx, double alpha, tagp
     c.st.ms_gemm = tm.ms();
   }
   fill_stats(c);
+  for (OzakiPlan* pl : c.ozs) c.st.mma_flops += ozaki_mma_flops(pl);
   c.st.kernel_launches = launch_count() - launches0;
   c.st.ms_total =
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -2209,6 +2493,13 @@ tagpu_status tagpu_batch_run(tagpu_batch* b) {
 tagpu_status tagpu_batch_stats(const tagpu_batch* b, tagpu_contract_stats* st) {
   if (!b || !st) return TAGPU_ERR_INVALID;
   *st = b->stats;
+  // the digit-slice products of the last run, read from the plans' counters
+  std::lock_guard<std::recursive_mutex> lk(b->ctx->mu);
+  cudaSetDevice(b->ctx->device);
+  st->mma_flops = 0;
+  for (const auto& en : b->entries)
+    if (en.plan)
+      for (OzakiPlan* pl : en.plan->ozs) st->mma_flops += ozaki_mma_flops(pl);
   return TAGPU_OK;
 }
 
