@@ -177,5 +177,30 @@ void ozaki_group_enqueue(const void* zero_jobs, const void* frame_jobs, const vo
 // two CTAs of a cluster); multi-view launches offset their views by these.
 int64_t ozaki_units(const OzakiPlan* pl);
 void ozaki_destroy(OzakiPlan* pl);
+// (unit, k block) stages of a plan: its GEMM work in stages of 32 k.
+int ozaki_stage_count(const OzakiPlan* pl);
+
+// Served mode: one persistent emulated GEMM (slice count S) that takes units
+// from a work queue.  Jobs (prepared plans) are published into lane 0 (short)
+// or lane 1 (long); lane 0 is claimed first.  Every call below is made by one
+// host thread.
+struct OzakiServe;
+// `reserve` co-resident clusters stay free for the kernels preparing requests.
+tagpu_status ozaki_serve_create(int S, int sm_count, int reserve, unsigned long long wait_ns,
+                                cudaStream_t stream, OzakiServe** out, std::string* err);
+void ozaki_serve_destroy(OzakiServe* q);   // stops the kernel, frees the queue
+int ozaki_serve_slices(const OzakiServe* q);
+// Frames, digit splits and stage shifts of a plan on stream s (no GEMM);
+// plans split in row chunks (ozaki_chunks > 1) are not served.
+void ozaki_prepare_served(OzakiPlan* pl, int sm_count, cudaStream_t s);
+// Publishes a prepared plan; returns its job id, -2 for a plan without units
+// (done at once), -1 when the job tables are full (reset first).
+int ozaki_serve_publish(OzakiServe* q, OzakiPlan* pl, int lane);
+bool ozaki_serve_done(const OzakiServe* q, int job);
+// Launches the kernel unless it runs.  *exited_error: the kernel had exited
+// with a bounded wait run out (its claimed jobs are lost; reset, then kick).
+tagpu_status ozaki_serve_kick(OzakiServe* q, int* exited_error, std::string* err);
+// With no job in flight: stops the kernel and restarts the job tables.
+tagpu_status ozaki_serve_reset(OzakiServe* q, std::string* err);
 
 }  // namespace tagpu

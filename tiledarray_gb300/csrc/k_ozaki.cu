@@ -338,6 +338,123 @@ struct Smem {
   static constexpr int kBytes = kStages * kStageBytes + 1024;
 };
 
+// ---------------------------------------------------------------------------
+// Served mode: a persistent GEMM that takes units from a work queue
+// ---------------------------------------------------------------------------
+// The host publishes jobs (one contraction plan each, already split into
+// digit bricks) into two lanes, 0 for short jobs and 1 for long ones.  The
+// lane's units are numbered in publication order; a cluster's leader (rank
+// 0 producer) claims the next unit of lane 0 if there is one, else of lane
+// 1, so a short job published while a long one runs starts on the next
+// cluster that finishes a unit.  Control words the host writes live in mapped
+// host memory; claim counters and per-job unit counts in device memory.
+constexpr int kQueueJobs = 1 << 16;   // jobs per lane between two resets
+struct QueueJob {
+  const void* view;          // the job's OzParams on the device
+  int64_t first;             // number of its first unit in its lane
+  int64_t units;             // units (pairs of output blocks)
+  int32_t id;                // completion slot
+  int32_t pad;
+};
+struct QueueArgs {
+  const QueueJob* jobs[2];           // per lane, publication order (mapped)
+  const volatile long long* published;   // [2] units published per lane (mapped)
+  const volatile int* njobs;         // [2] jobs published per lane (mapped)
+  const volatile int* stop;          // exit once nothing is left to claim (mapped)
+  volatile int* job_done;            // [2 * kQueueJobs] 1 once a job finished (mapped)
+  unsigned long long* claimed;       // [2] units claimed per lane (device)
+  int* done_units;                   // [2 * kQueueJobs] CTA-units finished per job (device)
+  unsigned long long idle_ns;        // exit after this long with nothing to claim
+};
+// A unit as the roles of a CTA see it; b < 0 ends the kernel.
+struct QUnit {
+  const OzParams* P;
+  long long b;
+  long long tag;             // job id | units << 20 (units < 2^43)
+};
+
+__device__ __forceinline__ long long ld_acquire_sys(const volatile long long* p) {
+  long long v;
+  asm volatile("ld.acquire.sys.global.s64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_acquire_sys(const volatile int* p) {
+  int v;
+  asm volatile("ld.acquire.sys.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+// Address of the same shared-memory location in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t mapa(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_cluster_u64(uint32_t addr, unsigned long long v) {
+  asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(addr)
+               : "memory");
+}
+// Bounded wait with cluster-scope acquire (the slot may have been written by
+// the partner CTA).
+__device__ __forceinline__ bool mbar_wait_cluster(uint32_t a, uint32_t parity,
+                                                  volatile int* abort_s,
+                                                  unsigned long long wait_ns) {
+  auto try1 = [&]() {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return ok != 0;
+  };
+  if (try1()) return true;
+  const uint64_t t0 = globaltimer();
+  for (uint32_t i = 0;; ++i) {
+    if (try1()) return true;
+    if ((i & 63) == 0) {
+      if (*abort_s) return false;
+      if (globaltimer() - t0 > wait_ns) return false;
+    }
+  }
+}
+// Claims the next unit (lane 0 before lane 1); false when there is none and
+// the host asked to stop, the kernel has been idle for idle_ns, or a role
+// aborted.  cache[l]: index of the lane's job the last claim fell into.
+__device__ bool queue_claim(const QueueArgs& q, QUnit& u, int* cache, volatile int* abort_s) {
+  const uint64_t t0 = globaltimer();
+  for (;;) {
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+      const long long pub = ld_acquire_sys(&q.published[l]);
+      unsigned long long c = *(volatile unsigned long long*)&q.claimed[l];
+      while ((long long)c < pub) {
+        const unsigned long long prev = atomicCAS(&q.claimed[l], c, c + 1);
+        if (prev == c) {
+          // the job holding unit c: jobs are published before their units
+          const int nj = ld_acquire_sys(&q.njobs[l]);
+          int j = cache[l] < nj ? cache[l] : nj - 1;
+          while (j + 1 < nj && q.jobs[l][j + 1].first <= (long long)c) ++j;
+          while (j > 0 && q.jobs[l][j].first > (long long)c) --j;
+          cache[l] = j;
+          const QueueJob& J = q.jobs[l][j];
+          u.P = static_cast<const OzParams*>(J.view);
+          u.b = (long long)c - J.first;
+          u.tag = (long long)J.id | (J.units << 20);
+          return true;
+        }
+        c = prev;
+      }
+    }
+    if (*abort_s || ld_acquire_sys(q.stop)) return false;
+    if (globaltimer() - t0 > q.idle_ns) return false;
+    __nanosleep(500);
+  }
+}
+
 // Output blocks of several contractions form one list: block gb belongs to
 // view v with vstart[v] <= gb < vstart[v+1].
 __device__ __forceinline__ int find_view(const int64_t* __restrict__ vstart, int nviews,
@@ -350,48 +467,92 @@ __device__ __forceinline__ int find_view(const int64_t* __restrict__ vstart, int
   return lo;
 }
 
-// The MMAs of one stage whose levels are all written already, for shift SH
-// and last level L known at compile time: slice p feeds levels
-// p+1+SH .. p+SH+min(L-p-SH, S) with B slices 1.., one MMA (two above N =
-// 256) per slice and k step, every descriptor a constant offset from the
-// stage's.  Descriptor address fields count 16-byte units.
+// MMAs of one stage with shift SH and last level L known at compile time:
+// slice p feeds levels p+1+SH .. p+SH+min(L-p-SH, S) with B slices 1..,
+// one MMA (two above N = 256) per slice and k step, every descriptor a
+// constant offset from the stage's (descriptor address fields count 16-byte
+// units).  Slices p0..p1 of k step ks, all with accumulate on.
 template <int S, int SH, int L>
-__device__ __forceinline__ void stage_mmas(uint32_t tmem, uint64_t ad0, uint64_t bd0) {
+__device__ __forceinline__ void slices_full(uint32_t tmem, uint64_t ad0, uint64_t bd0, int ks,
+                                            int p0, int p1) {
 #pragma unroll
-  for (int ks = 0; ks < 2; ++ks)
-#pragma unroll
-    for (int p = 1; p <= S; ++p) {
-      const int nl = L - p - SH < S ? L - p - SH : S;
-      if (nl > 0) {
-        const uint64_t ad = ad0 + (uint64_t)(((p - 1) * A_SLICE_BYTES + ks * 256) >> 4);
-        const uint64_t bd = bd0 + (uint64_t)((ks * 256) >> 4);
-        const uint32_t d = tmem + (p - 1 + SH) * BN;
-        const int nn = nl * BN;
-        if (nn <= 256) {
-          tc_mma(d, ad, bd, idesc_n(nn), 1u);
-        } else {
-          const int h = nn / 2;
-          tc_mma(d, ad, bd, idesc_n(h), 1u);
-          tc_mma(d + h, ad, bd + (uint64_t)(((h / 8) * 512) >> 4), idesc_n(h), 1u);
-        }
+  for (int p = 1; p <= S; ++p) {
+    const int nl = L - p - SH < S ? L - p - SH : S;
+    if (nl > 0 && p >= p0 && p <= p1) {
+      const uint64_t ad = ad0 + (uint64_t)((((p - 1) * A_SLICE_BYTES) >> 4) + ks * 16);
+      const uint64_t bd = bd0 + (uint64_t)(ks * 16);
+      const uint32_t d = tmem + (p - 1 + SH) * BN;
+      const int nn = nl * BN;
+      if (nn <= 256) {
+        tc_mma(d, ad, bd, idesc_n(nn), 1u);
+      } else {
+        const int h = nn / 2;
+        tc_mma(d, ad, bd, idesc_n(h), 1u);
+        tc_mma(d + h, ad, bd + (uint64_t)(((h / 8) * 512) >> 4), idesc_n(h), 1u);
       }
     }
+  }
+}
+// Levels lo..hi of slice 1, k step 0 (B slices from lo - 1 - SH).
+template <int S, int SH>
+__device__ __forceinline__ void slice1_run(uint32_t tmem, uint64_t ad0, uint64_t bd0, int lo,
+                                           int hi, uint32_t acc) {
+  if (hi < lo) return;
+  const uint64_t bd = bd0 + (uint64_t)(((lo - 2 - SH) * B_SLICE_BYTES) >> 4);
+  const uint32_t d = tmem + (lo - 2) * BN;
+  const int nn = (hi - lo + 1) * BN;
+  if (nn <= 256) {
+    tc_mma(d, ad0, bd, idesc_n(nn), acc);
+  } else {
+    const int h = nn / 2;
+    tc_mma(d, ad0, bd, idesc_n(h), acc);
+    tc_mma(d + h, ad0, bd + (uint64_t)(((h / 8) * 512) >> 4), idesc_n(h), acc);
+  }
+}
+// The three stage programs, for a stage with no fresh level among its own:
+//   kStageAll:     every slice (k step 0, then 1);
+//   kStageRestartA: at a stage restarting levels zlo..5, the slices whose
+//                  lowest level lies above 5 (issued before the wait);
+//   kStageRestartC: the rest once levels zlo..5 are free and marked fresh:
+//                  slice 1's k step 0 in three runs, the restarting run
+//                  [max(zlo, 2+SH), 5] with accumulate off, then the
+//                  remaining slices below level 6.
+enum { kStageAll = 0, kStageRestartA = 1, kStageRestartC = 2 };
+template <int S, int SH, int L, int KIND>
+__device__ __forceinline__ void stage_program(uint32_t tmem, uint64_t ad0, uint64_t bd0, int zlo) {
+  if constexpr (KIND == kStageAll) {
+    slices_full<S, SH, L>(tmem, ad0, bd0, 0, 1, S);
+    slices_full<S, SH, L>(tmem, ad0, bd0, 1, 1, S);
+  } else if constexpr (KIND == kStageRestartA) {
+    slices_full<S, SH, L>(tmem, ad0, bd0, 0, 5 - SH, S);
+    slices_full<S, SH, L>(tmem, ad0, bd0, 1, 5 - SH, S);
+  } else {
+    if constexpr (SH <= 3) {   // slice 1 starts at level 2 + SH <= 5
+      const int lo = 2 + SH, hi = (L < 1 + SH + S) ? L : 1 + SH + S;
+      const int f0 = zlo > lo ? zlo : lo;
+      slice1_run<S, SH>(tmem, ad0, bd0, lo, f0 - 1, 1u);
+      slice1_run<S, SH>(tmem, ad0, bd0, f0, hi < 5 ? hi : 5, 0u);
+      slice1_run<S, SH>(tmem, ad0, bd0, 6, hi, 1u);
+      slices_full<S, SH, L>(tmem, ad0, bd0, 0, 2, 4 - SH);
+      slices_full<S, SH, L>(tmem, ad0, bd0, 1, 1, 4 - SH);
+    }
+  }
 }
 // Selects the instance for a stage's shift s (0..S+1) and extra levels e.
-template <int S, int SH>
-__device__ __forceinline__ void stage_mmas_dispatch(int s, int e, uint32_t tmem, uint64_t ad0,
-                                                    uint64_t bd0) {
+template <int S, int SH, int KIND>
+__device__ __forceinline__ void stage_dispatch(int s, int e, uint32_t tmem, uint64_t ad0,
+                                               uint64_t bd0, int zlo) {
   if constexpr (SH <= S + 1) {
     if (s == SH) {
       if (e == 0) {
-        stage_mmas<S, SH, S + 1>(tmem, ad0, bd0);
+        stage_program<S, SH, S + 1, KIND>(tmem, ad0, bd0, zlo);
       } else if (e == 1) {
-        if constexpr (S + 2 <= 9) stage_mmas<S, SH, S + 2>(tmem, ad0, bd0);
+        if constexpr (S + 2 <= 9) stage_program<S, SH, S + 2, KIND>(tmem, ad0, bd0, zlo);
       } else {
-        if constexpr (S + 3 <= 9) stage_mmas<S, SH, S + 3>(tmem, ad0, bd0);
+        if constexpr (S + 3 <= 9) stage_program<S, SH, S + 3, KIND>(tmem, ad0, bd0, zlo);
       }
     } else {
-      stage_mmas_dispatch<S, SH + 1>(s, e, tmem, ad0, bd0);
+      stage_dispatch<S, SH + 1, KIND>(s, e, tmem, ad0, bd0, zlo);
     }
   }
 }
@@ -416,10 +577,11 @@ __device__ __forceinline__ void stage_mmas_dispatch(int s, int e, uint32_t tmem,
 // Lazy zeroing: a level restarts by being marked fresh; the first MMA that
 // writes a fresh level does so with accumulate off.  A level still fresh at a
 // drain got no product in its period, and the epilogue skips it.
-template <int S>
+template <int S, bool Q>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
     const OzParams* __restrict__ views, const int64_t* __restrict__ vstart, int nviews,
-    int64_t nblk_total, int* __restrict__ err, unsigned long long wait_ns) {
+    int64_t nblk_total, int* __restrict__ err, unsigned long long wait_ns,
+    const QueueArgs* __restrict__ qa) {
   constexpr int STAGES = Smem<S>::kStages;
   constexpr int STAGE_BYTES = Smem<S>::kStageBytes;
   // levels 2..TOP are MMA targets: S + 1 of them and up to two extra, as
@@ -432,6 +594,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
   __shared__ uint32_t tmem_base_s;
   __shared__ uint32_t fresh_ring[4];   // per drain: levels that got no product
   __shared__ volatile int abort_s;
+  // served mode: units handed from the cluster leader to the roles of both CTAs
+  __shared__ __align__(8) QUnit q_ring[4];
+  __shared__ __align__(8) uint64_t q_full[4], q_empty[4], epi_done;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint8_t* stage_base = (uint8_t*)(((uintptr_t)smem + 1023) & ~(uintptr_t)1023);
@@ -450,6 +615,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
     mbar_init(smem_u32(&bar_acc_full), 2);
     for (int t = 0; t <= TOP; ++t) mbar_init(smem_u32(&bar_level[t]), EPI_WARPS);  // per warp
     mbar_init(smem_u32(&bar_done), 1);
+    for (int i = 0; i < 4; ++i) {
+      mbar_init(smem_u32(&q_full[i]), 1);
+      // consumers of a slot: MMA + 8 epilogue warps of rank 0, producer, MMA
+      // and 8 epilogue warps of rank 1 (only rank 0's barrier is used)
+      mbar_init(smem_u32(&q_empty[i]), 19);
+    }
+    mbar_init(smem_u32(&epi_done), EPI_WARPS);
     abort_s = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -469,6 +641,35 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
     abort_s = 1;
     atomicCAS(err, 0, code);
   };
+  // Served mode, a consumer warp: the next unit from the ring; lane 0 then
+  // releases the slot to the cluster leader.  false ends the warp's loop.
+  int qslot = 0;
+  uint32_t qph = 0;
+  auto ring_read = [&](int slot) {
+    const volatile long long* w = reinterpret_cast<const volatile long long*>(&q_ring[slot]);
+    QUnit u;
+    u.P = reinterpret_cast<const OzParams*>(w[0]);
+    u.b = w[1];
+    u.tag = w[2];
+    return u;
+  };
+  auto ring_take = [&](QUnit& u) -> bool {
+    if (!mbar_wait_cluster(smem_u32(&q_full[qslot]), qph, &abort_s, wait_ns)) {
+      fail(6);
+      return false;
+    }
+    u = ring_read(qslot);
+    __syncwarp();
+    if (lane == 0) {
+      const uint32_t e = smem_u32(&q_empty[qslot]);
+      if (rank == 0) mbar_arrive(e); else mbar_arrive_cluster(mapa(e, 0));
+    }
+    if (++qslot == 4) {
+      qslot = 0;
+      qph ^= 1;
+    }
+    return u.b >= 0;
+  };
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
@@ -481,11 +682,63 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
     bool issued[STAGES];
     for (int s = 0; s < STAGES; ++s) issued[s] = false;
     bool ok = true;
-    for (int64_t gb = unit0; gb < nblk_total && ok; gb += unit_step) {
-      const int vi = find_view(vstart, nviews, gb);
-      const OzParams& P = views[vi];
-      const int64_t b = gb - vstart[vi];
+    // loads of one unit's stages
+    // A stage loads the slices its products use: slice p and B slice q meet
+    // on level p + q + s <= L, so a column block needs the first
+    // min(S, L - 1 - s) slices of both bricks.  The A prefix is the larger of
+    // the two column blocks' (both CTAs receive the multicast halves).
+    int64_t gb = unit0;
+    int cache[2] = {0, 0};
+    for (;;) {
+      // the next unit: the static stride, or (served) the cluster leader
+      // claims one and hands it to both CTAs through the ring
+      const OzParams* Pp = nullptr;
+      int64_t b = 0;
+      if constexpr (!Q) {
+        if (gb >= nblk_total || !ok) break;
+        const int vi = find_view(vstart, nviews, gb);
+        Pp = &views[vi];
+        b = gb - vstart[vi];
+        gb += unit_step;
+      } else if (rank == 0) {
+        QUnit u;
+        if (lane == 0) {
+          bool got = mbar_wait(smem_u32(&q_empty[qslot]), qph ^ 1, &abort_s, wait_ns);
+          if (!got) fail(7);
+          got = got && queue_claim(*qa, u, cache, &abort_s);
+          if (!got) {
+            u.P = nullptr;
+            u.b = -1;
+            u.tag = 0;
+          }
+          const uint32_t slot = smem_u32(&q_ring[qslot]);
+          const uint32_t rslot = mapa(slot, 1);
+          q_ring[qslot] = u;
+          st_cluster_u64(rslot, (unsigned long long)(uintptr_t)u.P);
+          st_cluster_u64(rslot + 8, (unsigned long long)u.b);
+          st_cluster_u64(rslot + 16, (unsigned long long)u.tag);
+          mbar_arrive(smem_u32(&q_full[qslot]));
+          mbar_arrive_cluster(mapa(smem_u32(&q_full[qslot]), 1));
+        }
+        __syncwarp();
+        u = ring_read(qslot);
+        if (++qslot == 4) {
+          qslot = 0;
+          qph ^= 1;
+        }
+        if (u.b < 0 || !ok) break;
+        Pp = u.P;
+        b = u.b;
+      } else {
+        QUnit u;
+        if (!ok || !ring_take(u)) break;
+        Pp = u.P;
+        b = u.b;
+      }
+      const OzParams& P = *Pp;
       const int64_t x0 = P.blk_rng[2 * b], x1 = P.blk_rng[2 * b + 1];
+      const int L0 = S + 1 + (int)((uint32_t)P.unitM[2 * b] >> 28);
+      const int L1 = S + 1 + (int)((uint32_t)P.unitM[2 * b + 1] >> 28);
       for (int64_t xb = x0; xb < x1 && ok; xb += 32) {
         int4 mine = make_int4(0, 0, 0, 0);
         if (xb + lane < x1) mine = P.blk_ab[xb + lane];
@@ -502,16 +755,21 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
             } else {
               uint8_t* dst = stage_base + stage * STAGE_BYTES;
               const uint32_t full = smem_u32(&bar_full[stage]);
-              // this CTA's half of the shared A brick into both CTAs, then its
-              // own B brick; the full stage (both A halves + B) completes here
-              constexpr uint32_t kHalfA = S * A_SLICE_BYTES / 2;   // multiple of 16
-              mbar_expect_tx(full, STAGE_BYTES);
-              bulk_g2s_mc(smem_u32(dst) + rank * kHalfA,
+              const int need0 = max(0, min(S, L0 - 1 - (w & 0xff)));
+              const int need1 = max(0, min(S, L1 - 1 - ((w >> 8) & 0xff)));
+              const int na = max(need0, need1), nb = rank ? need1 : need0;
+              // this CTA's half of the A prefix into both CTAs, then its own B
+              // prefix; the stage (both A halves + B) completes here
+              const uint32_t half_a = (uint32_t)na * (A_SLICE_BYTES / 2);   // multiple of 16
+              mbar_expect_tx(full, (uint32_t)(na * A_SLICE_BYTES + nb * B_SLICE_BYTES));
+              bulk_g2s_mc(smem_u32(dst) + rank * half_a,
                           P.Apack + (size_t)(sa - P.a_slot_base) * (S * A_SLICE_BYTES) +
-                              rank * kHalfA,
-                          kHalfA, full, (uint16_t)3);
-              bulk_g2s(smem_u32(dst + S * A_SLICE_BYTES),
-                       P.Bpack + (size_t)sb * (S * B_SLICE_BYTES), S * B_SLICE_BYTES, full);
+                              rank * half_a,
+                          half_a, full, (uint16_t)3);
+              if (nb > 0)
+                bulk_g2s(smem_u32(dst + S * A_SLICE_BYTES),
+                         P.Bpack + (size_t)sb * (S * B_SLICE_BYTES), (uint32_t)nb * B_SLICE_BYTES,
+                         full);
               issued[stage] = true;
               issued_parity[stage] = phase;
             }
@@ -603,10 +861,23 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
       level_used |= 1u << t;
       return true;
     };
-    for (int64_t gb = unit0; gb < nblk_total && ok; gb += unit_step) {
-      const int vi = find_view(vstart, nviews, gb);
-      const OzParams& P = views[vi];
-      const int64_t b = gb - vstart[vi];
+    int64_t gb = unit0;
+    for (;;) {
+      const OzParams* Pp = nullptr;
+      int64_t b = 0;
+      if constexpr (!Q) {
+        if (gb >= nblk_total || !ok) break;
+        const int vi = find_view(vstart, nviews, gb);
+        Pp = &views[vi];
+        b = gb - vstart[vi];
+        gb += unit_step;
+      } else {
+        QUnit u;
+        if (!ok || !ring_take(u)) break;
+        Pp = u.P;
+        b = u.b;
+      }
+      const OzParams& P = *Pp;
       const int64_t x0 = P.blk_rng[2 * b];
       const int64_t n = P.blk_rng[2 * b + 1] - x0;
       const int L = S + 1 + (int)((uint32_t)P.unitM[2 * b + rank] >> 28);
@@ -638,8 +909,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
               const uint32_t span = ((2u << L) - 1u) & ~((1u << (2 + s)) - 1u);
               if (!(fresh & span)) {
                 // common case: every level of the stage is written already
-                stage_mmas_dispatch<S, 0>(s, L - S - 1, tmem, make_desc(sbase),
-                                          make_desc(sbase + S * A_SLICE_BYTES));
+                stage_dispatch<S, 0, kStageAll>(s, L - S - 1, tmem, make_desc(sbase),
+                                                make_desc(sbase + S * A_SLICE_BYTES), 0);
               } else {
 #pragma unroll
                 for (int ks = 0; ks < 2; ++ks)
@@ -668,13 +939,23 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
             }
             if (!ok) break;
           } else {
+            // a restart of levels zlo..5 (periods end together at multiples
+            // of 8 stages, so z is always such a run)
             const int tmax = 31 - __clz(z);
+            const int zlo = __ffs(z) - 1;
+            const uint32_t span = ((2u << L) - 1u) & ~((1u << (2 + s)) - 1u);
+            const bool quick = S >= 4 && !(fresh & span) && tmax == 5;
+            const uint64_t ad0 = make_desc(sbase), bd0 = make_desc(sbase + S * A_SLICE_BYTES);
             if (lane == 0 && has) {
+              if (quick) {
+                stage_dispatch<S, 0, kStageRestartA>(s, L - S - 1, tmem, ad0, bd0, zlo);
+              } else {
 #pragma unroll
-              for (int ks = 0; ks < 2; ++ks)
+                for (int ks = 0; ks < 2; ++ks)
 #pragma unroll
-                for (int p = 1; p <= S; ++p)
-                  if (p + 1 + s > tmax && p + 1 + s <= L) issue(sbase, p, ks, s, L);
+                  for (int p = 1; p <= S; ++p)
+                    if (p + 1 + s > tmax && p + 1 + s <= L) issue(sbase, p, ks, s, L);
+              }
             }
             __syncwarp();
 #pragma unroll
@@ -687,11 +968,16 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
             if (!ok) break;
             fresh |= z;
             if (lane == 0 && has) {
+              if (quick) {
+                stage_dispatch<S, 0, kStageRestartC>(s, L - S - 1, tmem, ad0, bd0, zlo);
+                fresh &= ~span;
+              } else {
 #pragma unroll
-              for (int ks = 0; ks < 2; ++ks)
+                for (int ks = 0; ks < 2; ++ks)
 #pragma unroll
-                for (int p = 1; p <= S; ++p)
-                  if (p + 1 + s <= tmax && p + 1 + s <= L) issue(sbase, p, ks, s, L);
+                  for (int p = 1; p <= S; ++p)
+                    if (p + 1 + s <= tmax && p + 1 + s <= L) issue(sbase, p, ks, s, L);
+              }
             }
           }
           __syncwarp();
@@ -716,7 +1002,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
           }
         }
       }
-    }
+        }
     // nothing may be in flight when tensor memory is released
     if (lane == 0) tc_commit(smem_u32(&bar_done));
     __syncwarp();
@@ -745,10 +1031,26 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
     int64_t hi[32], lo[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j) hi[j] = lo[j] = 0;
-    for (int64_t gb = unit0; gb < nblk_total && ok; gb += unit_step) {
-      const int vi = find_view(vstart, nviews, gb);
-      const OzParams& P = views[vi];
-      const int64_t b = gb - vstart[vi];
+    int64_t gb = unit0;
+    uint32_t nunits = 0;
+    for (;;) {
+      const OzParams* Pp = nullptr;
+      int64_t b = 0;
+      long long tag = 0;
+      if constexpr (!Q) {
+        if (gb >= nblk_total || !ok) break;
+        const int vi = find_view(vstart, nviews, gb);
+        Pp = &views[vi];
+        b = gb - vstart[vi];
+        gb += unit_step;
+      } else {
+        QUnit u;
+        if (!ok || !ring_take(u)) break;
+        Pp = u.P;
+        b = u.b;
+        tag = u.tag;
+      }
+      const OzParams& P = *Pp;
       const int rb = P.blk[2 * b], cb = 2 * P.blk[2 * b + 1] + (int)rank;
       const int64_t n = P.blk_rng[2 * b + 1] - P.blk_rng[2 * b];
       for (int64_t x = 0; x < n; ++x) {
@@ -822,6 +1124,32 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
       }
 #pragma unroll
       for (int j = 0; j < 32; ++j) hi[j] = lo[j] = 0;
+          if constexpr (Q) {
+        // Each finished unit is counted per job once all eight warps have
+        // stored their results; the count reaching both CTAs of every unit
+        // marks the job done for the host.
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&epi_done));
+        if (warp == 2) {
+          if (!mbar_wait(smem_u32(&epi_done), nunits & 1u, &abort_s, wait_ns)) {
+            fail(8);
+            break;
+          }
+          if (lane == 0) {
+            const int job = (int)(tag & 0xFFFFF);
+            const long long units = tag >> 20;
+            __threadfence_system();
+            const int prev = atomicAdd(&qa->done_units[job], 1);
+            if ((long long)prev + 1 == 2 * units) {
+              __threadfence_system();
+              asm volatile("st.release.sys.global.s32 [%0], %1;" ::"l"(&qa->job_done[job]), "r"(1)
+                           : "memory");
+            }
+          }
+          __syncwarp();
+        }
+        ++nunits;
+      }
     }
   }
   tc_fence_before();
@@ -1455,22 +1783,6 @@ __global__ void slot_pairs_kernel(const int32_t* __restrict__ blk, const int64_t
   }
 }
 
-// Unit b's slot list rotated left by rot[b] (0 <= rot[b] < its length):
-// out[off[b] + j] = in[off[b] + (j + rot[b]) mod n].  One warp per unit.
-__global__ void rotate_units_kernel(const int4* __restrict__ in, const int64_t* __restrict__ off,
-                                    const int32_t* __restrict__ rot, int64_t nblk,
-                                    int4* __restrict__ out) {
-  const int lane = threadIdx.x & 31;
-  const int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (b >= nblk) return;
-  const int64_t o = off[b], n = off[b + 1] - o, r = rot[b];
-  for (int64_t j = lane; j < n; j += 32) {
-    int64_t x = j + r;
-    if (x >= n) x -= n;
-    out[o + j] = in[o + x];
-  }
-}
-
 __global__ void flag_nonzero_kernel(const int64_t* __restrict__ counts, int64_t n,
                                     int64_t* __restrict__ flag) {
   const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1580,19 +1892,18 @@ namespace {
 
 constexpr int kMaxDevices = 128;
 
-template <int S>
-void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int64_t nblk,
-                   int* err, int sm_count, unsigned long long wait_ns, cudaStream_t st) {
+// Co-resident clusters of the GEMM kernel on the current device (the
+// shared-memory attribute is set on first use, per device).
+template <int S, bool Q>
+int gemm_clusters(int sm_count) {
   const size_t smem = Smem<S>::kBytes;
-  // the shared-memory attribute and the co-resident cluster count are per
-  // device
   static bool set[kMaxDevices] = {};
   static int clusters[kMaxDevices] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= kMaxDevices) dev = 0;
   if (!set[dev]) {
-    cudaFuncSetAttribute(ozaki_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(ozaki_gemm_kernel<S, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     // A persistent grid larger than what fits at once would leave the extra
     // clusters to start after others finish their whole share.
@@ -1601,7 +1912,8 @@ void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int
     cfg.blockDim = dim3(THREADS, 1, 1);
     cfg.dynamicSmemBytes = smem;
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, ozaki_gemm_kernel<S>, &cfg) != cudaSuccess || n <= 0) {
+    if (cudaOccupancyMaxActiveClusters(&n, ozaki_gemm_kernel<S, Q>, &cfg) != cudaSuccess ||
+        n <= 0) {
       cudaGetLastError();
       n = sm_count / 2;
     }
@@ -1609,19 +1921,37 @@ void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int
     set[dev] = true;
     if (const char* e = getenv("TAGPU_VERBOSE"))
       if (atoi(e) > 0)
-        fprintf(stderr, "tagpu: emulated GEMM (S=%d) on device %d: %d co-resident clusters of 2 "
-                "(%d SMs)\n", S, dev, n, sm_count);
+        fprintf(stderr, "tagpu: emulated GEMM (S=%d%s) on device %d: %d co-resident clusters "
+                "of 2 (%d SMs)\n", S, Q ? ", served" : "", dev, n, sm_count);
   }
+  return clusters[dev];
+}
+
+template <int S>
+void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int64_t nblk,
+                   int* err, int sm_count, unsigned long long wait_ns, cudaStream_t st) {
+  const int clusters = gemm_clusters<S, false>(sm_count);
   // clusters of two CTAs, one unit (pair of output blocks) at a time each
-  const int64_t grid = 2 * std::min<int64_t>(nblk, clusters[dev]);
+  const int64_t grid = 2 * std::min<int64_t>(nblk, clusters);
   if (grid > 0) {
     // stage shifts from the digit bricks just split, then the GEMM
     shift_kernel<<<blocks_for(nblk * 32, 256), 256, 0, st>>>(views, vstart, nviews, nblk, S);
     count_launch();
-    ozaki_gemm_kernel<S><<<(unsigned)grid, THREADS, smem, st>>>(views, vstart, nviews, nblk, err,
-                                                                wait_ns);
+    ozaki_gemm_kernel<S, false><<<(unsigned)grid, THREADS, Smem<S>::kBytes, st>>>(
+        views, vstart, nviews, nblk, err, wait_ns, nullptr);
     count_launch();
   }
+}
+
+// The persistent served GEMM: all co-resident clusters but `reserve`, which
+// stay free for the kernels that prepare requests.
+template <int S>
+void launch_served_t(const QueueArgs* qa, int* err, int sm_count, int reserve,
+                     unsigned long long wait_ns, cudaStream_t st) {
+  const int clusters = std::max(1, gemm_clusters<S, true>(sm_count) - reserve);
+  ozaki_gemm_kernel<S, true><<<(unsigned)(2 * clusters), THREADS, Smem<S>::kBytes, st>>>(
+      nullptr, nullptr, 0, 0, err, wait_ns, qa);
+  count_launch();
 }
 
 // Dynamic shared memory of a split CTA: S staged slices of ROWS x 32 digits.
@@ -1769,51 +2099,6 @@ tagpu_status ozaki_schedule(OzakiPlan* pl, int gr, int gc, std::string* err) {
 
 // Plan: index maps, brick maps, block lists, scratch.  Host reads back only
 // the counts that size the allocations.
-// Rotations of the units' k lists for TAGPU_KPHASE (see ozaki_plan).
-tagpu_status kphase_rotate(OzakiPlan* pl, std::string* err) {
-  cudaStream_t s = pl->s;
-  constexpr int kGr = 4, kGc = 19, kClusters = 76, kUnitCost = 3;
-  const auto& hb = pl->h_blk;
-  const auto& ho = pl->h_off;
-  std::vector<int32_t> kb(pl->nkb);
-  if (pl->nkb) {
-    cudaMemcpyAsync(kb.data(), pl->blk_kb, kb.size() * 4, cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-  }
-  const int64_t nsc = ((pl->CB + 1) / 2 + kGc - 1) / kGc;
-  std::vector<std::pair<std::pair<int64_t, int64_t>, int64_t>> key(pl->nblk);
-  for (int64_t b = 0; b < pl->nblk; ++b) {
-    const int64_t rb = hb[2 * b], cp = hb[2 * b + 1];
-    key[b] = {{(rb / kGr) * nsc + cp / kGc, (cp % kGc) * kGr + rb % kGr}, b};
-  }
-  std::sort(key.begin(), key.end());
-  std::vector<int64_t> t(kClusters, 0);
-  std::vector<int32_t> rot(pl->nblk, 0);
-  for (int64_t i = 0; i < pl->nblk; ++i) {
-    const int64_t b = key[i].second, c = i % kClusters;
-    const int64_t o = ho[b], n = ho[b + 1] - o;
-    const int64_t k0 = t[c] % pl->KB;
-    int64_t r = 0;
-    while (r < n && kb[o + r] < k0) ++r;   // first k block at or after the phase
-    rot[b] = (int32_t)(r < n ? r : 0);
-    t[c] += n + kUnitCost;
-  }
-  int32_t* d_rot = nullptr;
-  int4* rotated = nullptr;
-  tagpu_status st;
-  if ((st = pl->upload(&d_rot, rot, err)) || (st = pl->alloc(&rotated, pl->nkb, err))) return st;
-  rotate_units_kernel<<<blocks_for(pl->nblk * 32, 256), 256, 0, s>>>(pl->blk_ab, pl->blk_off,
-                                                                     d_rot, pl->nblk, rotated);
-  count_launch();
-  pl->blk_ab = rotated;
-  const cudaError_t ce = cudaStreamSynchronize(s);
-  if (ce != cudaSuccess) {
-    *err = std::string("k-phase rotation: ") + cudaGetErrorString(ce);
-    return TAGPU_ERR_CUDA;
-  }
-  return TAGPU_OK;
-}
-
 tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
                         const int32_t* h_nsz, const int32_t* h_ksz, int slices,
                         OzakiPlan** out, std::string* err) {
@@ -2018,15 +2303,6 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
     cudaMemcpyAsync(pl->h_off.data(), pl->blk_off, pl->h_off.size() * 8, cudaMemcpyDeviceToHost,
                     s);
     cudaStreamSynchronize(s);
-  }
-  // Optional (TAGPU_KPHASE=1; not yet measured on the GPU): start every
-  // unit's k list at the k block its start time points to in the default
-  // schedule (76 clusters, 4 x 19 super-tiles, one time step per stage), so
-  // the clusters of a wave walk the same k blocks together and share them in
-  // L2.  The rotation depends on the unit alone, never on the tuned schedule
-  // or row chunking, so results stay identical across those.
-  if (const char* e = getenv("TAGPU_KPHASE")) {
-    if (atoi(e) > 0 && pl->nblk > 0 && (st = kphase_rotate(pl.get(), err))) return st;
   }
   if ((st = pl->alloc(&pl->blk_rng, 2 * pl->nblk, err))) return st;
   // operand slices (A: the largest chunk)
@@ -2328,5 +2604,217 @@ double ozaki_mma_flops(OzakiPlan* pl) {
 }
 int64_t ozaki_units(const OzakiPlan* pl) { return pl->nblk; }
 void ozaki_destroy(OzakiPlan* pl) { delete pl; }
+
+// ---------------------------------------------------------------------------
+// served mode (host side)
+// ---------------------------------------------------------------------------
+// Control block in mapped, page-locked host memory: the host publishes with
+// release stores, the kernel reads with acquire loads (the GPU of this
+// system is cache-coherent with host memory).
+struct ServeMapped {
+  long long published[2];
+  int njobs[2];
+  int stop;
+  int pad;
+  int job_done[2 * kQueueJobs];
+  QueueJob jobs[2][kQueueJobs];
+};
+
+struct OzakiServe {
+  int S = 6;
+  int sm_count = 0, reserve = 0;
+  unsigned long long wait_ns = 4000000000ull;
+  cudaStream_t stream = nullptr;     // the persistent kernel's stream
+  ServeMapped* h = nullptr;          // host view
+  ServeMapped* d = nullptr;          // device view of the same memory
+  unsigned long long* claimed = nullptr;
+  int* done_units = nullptr;
+  int* err = nullptr;
+  QueueArgs* d_args = nullptr;
+  cudaEvent_t ev = nullptr;          // recorded after each launch
+  bool running = false;
+  int next_id = 0;
+  long long lane_units[2] = {0, 0};
+  int lane_jobs[2] = {0, 0};
+  ~OzakiServe() {
+    if (running && h) {
+      __atomic_store_n(&h->stop, 1, __ATOMIC_RELEASE);
+      cudaStreamSynchronize(stream);
+    }
+    if (ev) cudaEventDestroy(ev);
+    if (d_args) cudaFree(d_args);
+    if (claimed) cudaFree(claimed);
+    if (done_units) cudaFree(done_units);
+    if (err) cudaFree(err);
+    if (h) cudaFreeHost(h);
+  }
+};
+
+tagpu_status ozaki_serve_create(int S, int sm_count, int reserve, unsigned long long wait_ns,
+                                cudaStream_t stream, OzakiServe** out, std::string* err) {
+  if (S < 2 || S > 7) {
+    *err = "served emulated form supports 2..7 slices";
+    return TAGPU_ERR_INVALID;
+  }
+  auto q = std::make_unique<OzakiServe>();
+  q->S = S;
+  q->sm_count = sm_count;
+  q->reserve = reserve;
+  q->wait_ns = wait_ns;
+  q->stream = stream;
+  void* hp = nullptr;
+  if (cudaHostAlloc(&hp, sizeof(ServeMapped), cudaHostAllocMapped) != cudaSuccess) {
+    cudaGetLastError();
+    *err = "served mode: mapped host control block allocation failed";
+    return TAGPU_ERR_NOMEM;
+  }
+  q->h = static_cast<ServeMapped*>(hp);
+  memset(q->h, 0, sizeof(ServeMapped));
+  void* dp = nullptr;
+  if (cudaHostGetDevicePointer(&dp, hp, 0) != cudaSuccess) {
+    cudaGetLastError();
+    *err = "served mode: mapped control block has no device address";
+    return TAGPU_ERR_CUDA;
+  }
+  q->d = static_cast<ServeMapped*>(dp);
+  if (cudaMalloc(&q->claimed, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&q->done_units, 2 * kQueueJobs * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&q->err, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&q->d_args, sizeof(QueueArgs)) != cudaSuccess) {
+    cudaGetLastError();
+    *err = "served mode: device allocation failed";
+    return TAGPU_ERR_NOMEM;
+  }
+  QueueArgs a{};
+  a.jobs[0] = q->d->jobs[0];
+  a.jobs[1] = q->d->jobs[1];
+  a.published = q->d->published;
+  a.njobs = q->d->njobs;
+  a.stop = &q->d->stop;
+  a.job_done = q->d->job_done;
+  a.claimed = q->claimed;
+  a.done_units = q->done_units;
+  a.idle_ns = 20000000ull;   // a kernel with nothing to claim for 20 ms exits
+  cudaMemcpyAsync(q->d_args, &a, sizeof(a), cudaMemcpyHostToDevice, stream);
+  cudaMemsetAsync(q->claimed, 0, 2 * sizeof(unsigned long long), stream);
+  cudaMemsetAsync(q->done_units, 0, 2 * kQueueJobs * sizeof(int), stream);
+  cudaMemsetAsync(q->err, 0, sizeof(int), stream);
+  cudaEventCreateWithFlags(&q->ev, cudaEventDisableTiming);
+  if (cudaStreamSynchronize(stream) != cudaSuccess) {
+    const cudaError_t ce = cudaGetLastError();
+    *err = std::string("served mode setup: ") + cudaGetErrorString(ce);
+    return TAGPU_ERR_CUDA;
+  }
+  *out = q.release();
+  return TAGPU_OK;
+}
+
+void ozaki_serve_destroy(OzakiServe* q) { delete q; }
+
+// Frames, digit splits and stage shifts of a plan on stream s, for a served
+// job (its GEMM runs in the served kernel).  Plans split in row chunks are
+// not served.
+void ozaki_prepare_served(OzakiPlan* pl, int sm_count, cudaStream_t s) {
+  ozaki_enqueue(pl, sm_count, s);
+  if (pl->nblk > 0) {
+    shift_kernel<<<blocks_for(pl->nblk * 32, 256), 256, 0, s>>>(pl->d_params, pl->d_vstart, 1,
+                                                                pl->nblk, pl->S);
+    count_launch();
+  }
+}
+
+int ozaki_serve_publish(OzakiServe* q, OzakiPlan* pl, int lane) {
+  if (pl->nblk <= 0) return -2;   // nothing to run: done at once
+  if (q->next_id >= 2 * kQueueJobs || q->lane_jobs[lane] >= kQueueJobs) return -1;
+  const int id = q->next_id++;
+  const int j = q->lane_jobs[lane]++;
+  QueueJob& J = q->h->jobs[lane][j];
+  J.view = pl->d_params;
+  J.first = q->lane_units[lane];
+  J.units = pl->nblk;
+  J.id = id;
+  J.pad = 0;
+  q->lane_units[lane] += pl->nblk;
+  __atomic_store_n(&q->h->njobs[lane], j + 1, __ATOMIC_RELEASE);
+  __atomic_store_n(&q->h->published[lane], q->lane_units[lane], __ATOMIC_RELEASE);
+  return id;
+}
+
+bool ozaki_serve_done(const OzakiServe* q, int job) {
+  return job < 0 || __atomic_load_n(&q->h->job_done[job], __ATOMIC_ACQUIRE) != 0;
+}
+
+// Launches the served kernel unless it is running; a kernel that has exited
+// reports its error flag (0: it ran out of work, else a bounded wait ran out
+// and the jobs it held are lost).
+tagpu_status ozaki_serve_kick(OzakiServe* q, int* exited_error, std::string* err) {
+  *exited_error = 0;
+  if (q->running) {
+    const cudaError_t ce = cudaEventQuery(q->ev);
+    if (ce == cudaErrorNotReady) return TAGPU_OK;
+    q->running = false;
+    if (ce != cudaSuccess) {
+      cudaGetLastError();
+      *err = std::string("served GEMM: ") + cudaGetErrorString(ce);
+      return TAGPU_ERR_CUDA;
+    }
+    int e = 0;
+    cudaMemcpyAsync(&e, q->err, sizeof(int), cudaMemcpyDeviceToHost, q->stream);
+    cudaMemsetAsync(q->err, 0, sizeof(int), q->stream);
+    cudaStreamSynchronize(q->stream);
+    *exited_error = e;
+  }
+  if (*exited_error) return TAGPU_OK;   // the caller fails the lost jobs, then kicks again
+  __atomic_store_n(&q->h->stop, 0, __ATOMIC_RELEASE);
+  switch (q->S) {
+    case 2: launch_served_t<2>(q->d_args, q->err, q->sm_count, q->reserve, q->wait_ns, q->stream); break;
+    case 3: launch_served_t<3>(q->d_args, q->err, q->sm_count, q->reserve, q->wait_ns, q->stream); break;
+    case 4: launch_served_t<4>(q->d_args, q->err, q->sm_count, q->reserve, q->wait_ns, q->stream); break;
+    case 5: launch_served_t<5>(q->d_args, q->err, q->sm_count, q->reserve, q->wait_ns, q->stream); break;
+    case 7: launch_served_t<7>(q->d_args, q->err, q->sm_count, q->reserve, q->wait_ns, q->stream); break;
+    default: launch_served_t<6>(q->d_args, q->err, q->sm_count, q->reserve, q->wait_ns, q->stream); break;
+  }
+  const cudaError_t le = cudaGetLastError();
+  if (le != cudaSuccess) {
+    *err = std::string("served GEMM launch: ") + cudaGetErrorString(le);
+    return TAGPU_ERR_CUDA;
+  }
+  cudaEventRecord(q->ev, q->stream);
+  q->running = true;
+  return TAGPU_OK;
+}
+
+// With no job in flight: the kernel is stopped (it exits at once, nothing is
+// left to claim) and the counters go back to zero so the job tables start
+// over.
+tagpu_status ozaki_serve_reset(OzakiServe* q, std::string* err) {
+  if (!q->running && q->next_id == 0) return TAGPU_OK;
+  if (q->running) {
+    __atomic_store_n(&q->h->stop, 1, __ATOMIC_RELEASE);
+    cudaStreamSynchronize(q->stream);
+    q->running = false;
+  }
+  const int used = q->next_id;
+  __atomic_store_n(&q->h->published[0], 0ll, __ATOMIC_RELEASE);
+  __atomic_store_n(&q->h->published[1], 0ll, __ATOMIC_RELEASE);
+  __atomic_store_n(&q->h->njobs[0], 0, __ATOMIC_RELEASE);
+  __atomic_store_n(&q->h->njobs[1], 0, __ATOMIC_RELEASE);
+  memset(q->h->job_done, 0, sizeof(int) * (size_t)std::max(used, 0));
+  cudaMemsetAsync(q->claimed, 0, 2 * sizeof(unsigned long long), q->stream);
+  if (used > 0) cudaMemsetAsync(q->done_units, 0, sizeof(int) * (size_t)used, q->stream);
+  cudaMemsetAsync(q->err, 0, sizeof(int), q->stream);
+  const cudaError_t ce = cudaStreamSynchronize(q->stream);
+  q->next_id = 0;
+  q->lane_units[0] = q->lane_units[1] = 0;
+  q->lane_jobs[0] = q->lane_jobs[1] = 0;
+  if (ce != cudaSuccess) {
+    *err = std::string("served mode reset: ") + cudaGetErrorString(ce);
+    return TAGPU_ERR_CUDA;
+  }
+  return TAGPU_OK;
+}
+
+int ozaki_serve_slices(const OzakiServe* q) { return q->S; }
+int ozaki_stage_count(const OzakiPlan* pl) { return (int)std::min<int64_t>(pl->nkb, 1 << 30); }
 
 }  // namespace tagpu

@@ -2671,10 +2671,16 @@ struct tagpu_server {
     tagpu_array* C = nullptr;
     tagpu_request_result res{};
     std::unique_ptr<Contraction> plan;
+    cudaEvent_t prep = nullptr;   // served: the preparation kernels are done
+    std::vector<int> jobs;        // served: job ids of its plans
+    ~Req() {
+      if (prep) cudaEventDestroy(prep);
+    }
   };
   tagpu_ctx* ctx = nullptr;
   tagpu_server_config cfg{};
-  cudaStream_t gemm_stream = nullptr;
+  cudaStream_t gemm_stream = nullptr;   // the persistent served GEMM
+  OzakiServe* served = nullptr;
   std::thread worker;
   std::mutex m;
   std::condition_variable cv, done_cv;
@@ -2730,44 +2736,55 @@ size_t footprint_bound(tagpu_array* A, const std::vector<std::string>& ai, tagpu
 
 }  // namespace
 
+// The request loop.  Admitted emulated requests are planned and prepared
+// (screening, pair list, frames, digit bricks, stage shifts) on the
+// context's stream, then published as jobs into the persistent served GEMM's
+// work queue: short jobs into the lane its clusters take first, so a small
+// request admitted while a large one runs starts as soon as any cluster
+// finishes its current unit.  A request completes when all its jobs are
+// counted done (and its post-permutation, if any, has run).  Other requests
+// (plain FP64, emulated plans built in row chunks or with another slice
+// count) run on the context's stream at once; they share the GPU with the
+// served kernel, which leaves a few clusters free for them and for the
+// preparation kernels.
 void tagpu_server::run() {
-  std::vector<std::shared_ptr<Req>> inflight;  // GEMMs enqueued on gemm_stream
-  LaunchBufs lb_a(ctx), lb_b(ctx);
-  LaunchBufs* inflight_lb = nullptr;   // the buffers of the batch in flight
-  bool use_a = true;
-  auto finish_inflight = [&]() {
-    if (inflight.empty()) return;
-    cudaError_t ce = cudaStreamSynchronize(gemm_stream);
-    // a bounded wait that ran out in a grouped launch invalidates its batch
-    const bool timed_out = ce == cudaSuccess && inflight_lb && inflight_lb->any_error();
+  std::deque<std::shared_ptr<Req>> prepping, serving;
+  LaunchBufs lb(ctx);
+  const int S = cfg.slices;
+  // jobs of at most this many (unit, k block) stages go to the first lane:
+  // about 0.3 ms of the whole GPU
+  constexpr int kShortStages = 76 * 256;
+  constexpr int kReserve = 4;   // clusters left free for other kernels
+  std::string err;
+  int64_t wave = 0;   // requests published so far (batch ids of served requests)
+  auto finish = [&](const std::shared_ptr<Req>& r, tagpu_status st) {
     const double t = now_ms();
     std::lock_guard<std::mutex> lk(m);
-    for (auto& r : inflight) {
+    r->res.status = st;
+    if (st == TAGPU_OK) {
       Contraction& c = *r->plan;
-      r->res.status = ce == cudaSuccess ? TAGPU_OK : TAGPU_ERR_CUDA;
-      if (r->res.status == TAGPU_OK && timed_out) r->res.status = TAGPU_ERR_TIMEOUT;
-      if (r->res.status == TAGPU_OK) {
-        fill_stats(c);
-        r->C = c.Cfinal ? c.Cfinal.release() : c.C.release();
-        r->res.flops = c.flops;
-        r->res.pairs = c.npairs;
-        flops += c.flops;
-        ++completed;
-        lat.push_back(t - r->t_submit);
-      } else {
-        ++failed;
-      }
-      r->res.latency_ms = t - r->t_submit;
-      r->plan.reset();
-      // the result stays in HBM until the client takes it: it keeps its
-      // bytes of the admission budget until then
-      r->held = r->C ? r->C->bytes : 0;
-      in_use -= r->bound;
-      in_use += r->held;
-      r->done = true;
-      t_last = t;
+      fill_stats(c);
+      r->C = c.Cfinal ? c.Cfinal.release() : c.C.release();
+      r->res.flops = c.flops;
+      r->res.pairs = c.npairs;
+      flops += c.flops;
+      ++completed;
+      lat.push_back(t - r->t_submit);
+    } else {
+      ++failed;
     }
-    inflight.clear();
+    r->res.latency_ms = t - r->t_submit;
+    {
+      std::lock_guard<std::recursive_mutex> lk2(ctx->mu);
+      r->plan.reset();
+    }
+    // the result stays in HBM until the client takes it: it keeps its bytes
+    // of the admission budget until then
+    r->held = r->C ? r->C->bytes : 0;
+    in_use -= r->bound;
+    in_use += r->held;
+    r->done = true;
+    t_last = t;
     done_cv.notify_all();
     cv.notify_all();
   };
@@ -2775,8 +2792,11 @@ void tagpu_server::run() {
     std::vector<std::shared_ptr<Req>> batch;
     {
       std::unique_lock<std::mutex> lk(m);
-      cv.wait(lk, [&] { return stopping || !queue.empty() || !inflight.empty(); });
-      if (stopping && queue.empty() && inflight.empty()) break;
+      const bool busy = !prepping.empty() || !serving.empty();
+      if (!busy) {
+        cv.wait(lk, [&] { return stopping || !queue.empty(); });
+        if (stopping && queue.empty()) break;
+      }
       const size_t budget = cfg.hbm_budget_bytes;
       const int maxb = cfg.max_batch > 0 ? cfg.max_batch : 64;
       for (auto it = queue.begin(); it != queue.end() && (int)batch.size() < maxb;) {
@@ -2790,7 +2810,7 @@ void tagpu_server::run() {
           ++it;
         }
       }
-      if (batch.empty() && inflight.empty()) {
+      if (batch.empty() && !busy && !queue.empty()) {
         if (stopping) {
           // results nobody took hold the budget: the queue can never run
           for (auto& r : queue) {
@@ -2803,68 +2823,150 @@ void tagpu_server::run() {
           done_cv.notify_all();
           break;
         }
-        // nothing fits until a client takes a result (or a request arrives)
-        cv.wait(lk);
+        // nothing fits until a client takes a result
+        cv.wait_for(lk, std::chrono::milliseconds(5));
         continue;
       }
     }
-    // plan the admitted requests while the previous batch is on the GPU
-    std::vector<Contraction*> cs;
-    std::vector<std::shared_ptr<Req>> ok;
-    {
-      std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-      cudaSetDevice(ctx->device);
-      for (auto& r : batch) {
+    // plan and prepare the admitted requests
+    for (auto& r : batch) {
+      r->res.queue_ms = r->t_admit - r->t_submit;
+      tagpu_status e;
+      bool servable = false;
+      {
+        std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+        cudaSetDevice(ctx->device);
         r->plan.reset(new Contraction(ctx));
-        tagpu_status e = plan_all(*r->plan, r->c.c_str(), r->alpha, r->A, r->a.c_str(), r->B,
-                                  r->b.c_str(), &r->opts);
-        if (e) {
-          std::lock_guard<std::mutex> lk2(m);
-          r->res.status = e;
-          r->res.latency_ms = now_ms() - r->t_submit;
-          r->plan.reset();
-          in_use -= r->bound;
-          r->done = true;
-          ++failed;
-          done_cv.notify_all();
-          continue;
+        e = plan_all(*r->plan, r->c.c_str(), r->alpha, r->A, r->a.c_str(), r->B, r->b.c_str(),
+                     &r->opts);
+        Contraction& c = *r->plan;
+        if (!e && c.emulated()) {
+          servable = true;
+          for (OzakiPlan* pl : c.ozs)
+            servable = servable && ozaki_chunks(pl) == 1 && ozaki_slices(pl) == S;
         }
-        cs.push_back(r->plan.get());
-        ok.push_back(r);
+        if (!e && servable && !served) {
+          e = ozaki_serve_create(S, ctx->sm_count, kReserve, ctx->wait_ns, gemm_stream, &served,
+                                 &err);
+          if (e) fail(ctx, e, "%s", err.c_str());
+        }
+        if (!e && servable) {
+          for (OzakiPlan* pl : c.ozs) ozaki_prepare_served(pl, ctx->sm_count, ctx->stream);
+          if (cudaEventCreateWithFlags(&r->prep, cudaEventDisableTiming) != cudaSuccess ||
+              cudaEventRecord(r->prep, ctx->stream) != cudaSuccess) {
+            cudaGetLastError();
+            e = TAGPU_ERR_CUDA;
+          }
+        } else if (!e) {
+          // not served: its own launches on the context's stream, now
+          std::vector<Contraction*> one{&c};
+          e = enqueue_gemms(ctx, one, lb, true, ctx->stream);
+          if (!e && c.post) c.post->enqueue(ctx->stream, c.post_in, c.post_out);
+          if (!e && cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+            cudaGetLastError();
+            e = TAGPU_ERR_CUDA;
+          }
+          if (!e && lb.any_error()) e = TAGPU_ERR_TIMEOUT;
+          ++batches;
+          r->res.batch_size = 1;
+          r->res.batch_id = next_batch++;
+        }
+      }
+      if (e || !servable) {
+        finish(r, e);
+        continue;
+      }
+      prepping.push_back(r);
+    }
+    // publish the requests whose preparation has finished (in admission order)
+    bool published = false;
+    while (!prepping.empty()) {
+      auto& r = prepping.front();
+      const cudaError_t q = cudaEventQuery(r->prep);
+      if (q == cudaErrorNotReady) break;
+      if (q != cudaSuccess) {
+        cudaGetLastError();
+        auto rr = r;
+        prepping.pop_front();
+        finish(rr, TAGPU_ERR_CUDA);
+        continue;
+      }
+      Contraction& c = *r->plan;
+      std::vector<int> ids;
+      bool full = false;
+      for (OzakiPlan* pl : c.ozs) {
+        const int lane = ozaki_stage_count(pl) <= kShortStages ? 0 : 1;
+        const int id = ozaki_serve_publish(served, pl, lane);
+        if (id == -1) {
+          full = true;   // tables full: published jobs of this request stay valid
+          break;
+        }
+        ids.push_back(id);
+      }
+      r->jobs.insert(r->jobs.end(), ids.begin(), ids.end());
+      if (full) break;   // the rest after the next reset
+      r->res.batch_id = (uint64_t)++wave;
+      serving.push_back(r);
+      prepping.pop_front();
+      published = true;
+    }
+    // keep the served kernel running while jobs are out
+    if (!serving.empty() && served) {
+      int exited_error = 0;
+      tagpu_status e = ozaki_serve_kick(served, &exited_error, &err);
+      if (e || exited_error) {
+        // a bounded wait ran out (or the launch failed): the jobs out are lost
+        while (!serving.empty()) {
+          auto r = serving.front();
+          serving.pop_front();
+          finish(r, e ? e : TAGPU_ERR_TIMEOUT);
+        }
+        ozaki_serve_reset(served, &err);
       }
     }
-    // the previous batch must be done before its buffers are reused
-    finish_inflight();
-    if (!ok.empty()) {
-      std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-      cudaSetDevice(ctx->device);
-      LaunchBufs& lb = use_a ? lb_a : lb_b;
-      use_a = !use_a;
-      tagpu_status e = enqueue_gemms(ctx, cs, lb, true, gemm_stream);
-      inflight_lb = &lb;
-      const uint64_t bid = next_batch++;
-      for (auto& r : ok) {
-        r->res.batch_size = (int)ok.size();
-        r->res.batch_id = bid;
-        r->res.queue_ms = r->t_admit - r->t_submit;
+    (void)published;
+    // completions
+    for (auto it = serving.begin(); it != serving.end();) {
+      auto r = *it;
+      bool all = true;
+      for (int id : r->jobs) all = all && ozaki_serve_done(served, id);
+      if (!all) {
+        ++it;
+        continue;
       }
-      ++batches;
-      if (e) {
-        std::lock_guard<std::mutex> lk2(m);
-        for (auto& r : ok) {
-          r->res.status = e;
-          r->plan.reset();
-          in_use -= r->bound;
-          r->done = true;
-          ++failed;
+      tagpu_status e = TAGPU_OK;
+      {
+        std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+        cudaSetDevice(ctx->device);
+        Contraction& c = *r->plan;
+        if (c.post) {
+          c.post->enqueue(ctx->stream, c.post_in, c.post_out);
+          if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+            cudaGetLastError();
+            e = TAGPU_ERR_CUDA;
+          }
         }
-        done_cv.notify_all();
-      } else {
-        inflight = ok;
       }
+      r->res.batch_size = (int)serving.size();   // requests on the GPU together
+      it = serving.erase(it);
+      finish(r, e);
+    }
+    // with nothing out, the job tables start over
+    if (served && serving.empty() && prepping.empty()) {
+      std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+      ozaki_serve_reset(served, &err);
+      ++batches;
+    }
+    if (!serving.empty() || !prepping.empty()) {
+      // poll the completion flags; new arrivals wake the loop at once
+      std::unique_lock<std::mutex> lk(m);
+      cv.wait_for(lk, std::chrono::microseconds(50));
     }
   }
-  finish_inflight();
+  if (served) {
+    ozaki_serve_destroy(served);
+    served = nullptr;
+  }
 }
 
 extern "C" {
