@@ -705,15 +705,16 @@ def main():
                 "mma_flops_per_step": mma,
                 "fp64_equivalent": {"achieved": flops * pairs_per / (gemm_ms * 1e-3) / 1e12,
                                     "note": f"{pairs_per} slice products per FP64 product"}}
-        if args.n == 16384 and args.seed == 0:
-            tb = profiled_traffic("ozaki_gemm_blocksparse.md")
+        if args.n == 16384 and args.slices == 7 and args.seed == 0:
+            tb = profiled_traffic("ozaki_gemm_blocksparse_n8192_s7.md")
             if tb:
                 roof["traffic"] = tb
                 roof["traffic_note"] = (
-                    "DRAM bytes of this launch from one ncu capture of the same command "
-                    f"(profiles/ozaki_gemm_blocksparse.md): {tb / (gemm_ms * 1e-3) / 1e9:.0f} "
-                    f"GB/s over the timed GEMM = {tb / (gemm_ms * 1e-3) / 1e9 / hbm_peak:.2f} "
-                    "of measured HBM")
+                    "DRAM bytes per launch estimated from one ncu capture of the same "
+                    "kernel at N=8192 scaled by the issued MMA work "
+                    f"(profiles/ozaki_gemm_blocksparse_n8192_s7.md): "
+                    f"{tb / (gemm_ms * 1e-3) / 1e9:.0f} GB/s over the timed GEMM = "
+                    f"{tb / (gemm_ms * 1e-3) / 1e9 / hbm_peak:.2f} of {peak_kind} HBM")
     else:
         achieved = flops / (gemm_ms * 1e-3) / 1e12
         dmma_peak, _ = w.fp64_rates()
