@@ -517,39 +517,58 @@ def run_secondary(args):
 def run_serve(args, w, ta, wl, prec):
     """Poisson request stream over the block-sparse, ccsd-like and batched
     families at scales U[0.25,1]; operands pre-generated and resident; the
-    server admits by footprint under a 150 GB budget."""
+    server admits by footprint under a 150 GB budget.
+
+    Operands come from a pool drawn once: block-sparse products at four
+    scales, ccsd-like contractions at scales spread over [0.25, 1] and
+    batched-family contractions.  A ccsd-like request whose footprint (digit
+    bricks of V dominate) can never fit the budget exists as arrays with a
+    shape but no storage and must come back rejected.  Requests pick a family
+    (weights --mix) and then a pool entry of it uniformly.  A sample of the
+    served results (those under 0.5 TFLOP) is checked against the plain FP64
+    form after the stream."""
     import threading
     rng = np.random.default_rng(args.seed)
     thr = 1e-8
-    pool = []
-    for x in range(4):   # block-sparse family
-        s = rng.uniform(0.25, 1.0)
-        h, scale = wl.blocksparse(int(16384 * s) // 64 * 64, seed=100 + x)
+    pool = {"blocksparse": [], "ccsd": [], "batched": []}
+    for x in range(4):
+        sc = rng.uniform(0.25, 1.0)
+        h, scale = wl.blocksparse(int(16384 * sc) // 64 * 64, seed=100 + x)
         tr = ta.TiledRange([h, h])
         A, B = ta.DistArray(w, tr), ta.DistArray(w, tr)
         A.generate(100 + x, 0, 0, scale, True, thr)
         B.generate(100 + x, 1, 0, scale, True, thr)
-        pool.append(("i,j", A, "i,k", B, "k,j", f"blocksparse s={s:.2f}"))
-    for x in range(3):   # ccsd-like family (v up to 192 resident: V <= 11 GB)
-        s = rng.uniform(0.25, 0.5)
-        hv, ho, vs, ts = wl.ccsd(o=int(48 * s) // 4 * 4 or 8, v=int(384 * s), seed=200 + x)
+        pool["blocksparse"].append(("i,j", A, "i,k", B, "k,j", f"blocksparse s={sc:.2f}"))
+    budget = 150 * 10 ** 9
+    for x, sc in enumerate(np.linspace(0.25, 1.0, 6)):
+        o = max(8, int(48 * sc) // 4 * 4)
+        hv, ho, vs, ts = wl.ccsd(o=o, v=int(384 * sc), seed=200 + x)
         V = ta.DistArray(w, ta.TiledRange([hv, hv, hv, hv]))
         T = ta.DistArray(w, ta.TiledRange([hv, hv, ho, ho]))
-        V.generate(200 + x, 0, 0, vs, True, thr)
-        T.generate(200 + x, 1, 0, ts, True, thr)
-        pool.append(("a,b,i,j", V, "a,b,c,d", T, "c,d,i,j", f"ccsd s={s:.2f}"))
-    for x, (tsl, ka, kb) in enumerate(wl.batched(8, seed=300)):   # batched family
+        v = int(384 * sc)
+        # V's digit bricks alone: v^4 elements x 2 bytes x slices
+        if v ** 4 * 2 * args.slices < budget:
+            V.generate(200 + x, 0, 0, vs, True, thr)
+            T.generate(200 + x, 1, 0, ts, True, thr)
+        # else: never admitted (its footprint bound, from the extents, exceeds the
+        # budget): the arrays exist without storage
+        pool["ccsd"].append(("a,b,i,j", V, "a,b,c,d", T, "c,d,i,j", f"ccsd s={sc:.2f}"))
+    for x, (tsl, ka, kb) in enumerate(wl.batched(8, seed=300)):
         A = ta.DistArray(w, ta.TiledRange([tsl[0], tsl[1], tsl[2]]))
         B = ta.DistArray(w, ta.TiledRange([tsl[2], tsl[3]]))
         A.generate(300 + x, 0, 0, ka, True)
         B.generate(300 + x, 1, 0, kb, True)
-        pool.append(("i,j,l", A, "i,j,k", B, "k,l", "batched"))
+        pool["batched"].append(("i,j,l", A, "i,j,k", B, "k,l", "batched"))
     w.threshold = thr
-    srv = ta.Server(w, hbm_budget_bytes=150 << 30, max_batch=32, precision=prec,
+    fams = ["blocksparse", "ccsd", "batched"]
+    mix = np.asarray([float(x) for x in args.mix.split(",")])
+    mix = mix / mix.sum()
+    srv = ta.Server(w, hbm_budget_bytes=budget, max_batch=32, precision=prec,
                     slices=args.slices)
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, args.requests))
-    picks = rng.integers(0, len(pool), args.requests)
-    ids, rejected = [None] * args.requests, [0]
+    fam_pick = rng.choice(3, size=args.requests, p=mix)
+    picks = [pool[fams[f]][int(rng.integers(0, len(pool[fams[f]])))] for f in fam_pick]
+    ids, rejected = [None] * args.requests, {}
     t0 = time.perf_counter()
     submitted = [0]
 
@@ -558,16 +577,18 @@ def run_serve(args, w, ta, wl, prec):
             dt = arrivals[x] - (time.perf_counter() - t0)
             if dt > 0:
                 time.sleep(dt)
-            c, A, a, B, b, _ = pool[picks[x]]
+            c, A, a, B, b, name = picks[x]
             try:
                 ids[x] = srv.submit(c, 1.0, A, a, B, b)
-            except ta.TAGPUError:
-                rejected[0] += 1
+            except ta.TAGPUError as e:
+                key = f"{name}: status {e.status}"
+                rejected[key] = rejected.get(key, 0) + 1
             submitted[0] = x + 1
 
     # the clients take their results as they complete (in submission order),
-    # so finished results do not pile up in HBM
-    results, failures = [], {}
+    # so finished results do not pile up in HBM; a sample is kept for the
+    # check against the plain form
+    results, failures, kept = [], {}, []
 
     def collector():
         for x in range(args.requests):
@@ -575,11 +596,21 @@ def run_serve(args, w, ta, wl, prec):
                 time.sleep(0.0005)
             if ids[x] is None:
                 continue
-            C, res = srv.wait(ids[x], 600000)
+            try:
+                C, res = srv.wait(ids[x], 600000)
+            except ta.TAGPUError as e:
+                # the request failed on the device side (its status and the
+                # server's message); the stream goes on
+                key = f"{picks[x][5]}: status {e.status}"
+                failures[key] = failures.get(key, 0) + 1
+                continue
             results.append(res)
             if res["status"] != 0:
-                key = f"{pool[picks[x]][5]}: status {res['status']}"
+                key = f"{picks[x][5]}: status {res['status']}"
                 failures[key] = failures.get(key, 0) + 1
+            elif len(kept) < args.check and res["flops"] < 5e11 and x % 7 == 0:
+                kept.append((x, C))
+                continue
             del C
     th = threading.Thread(target=submitter)
     tc = threading.Thread(target=collector)
@@ -590,17 +621,29 @@ def run_serve(args, w, ta, wl, prec):
     wall = time.perf_counter() - t0
     st = srv.stats()
     srv.stop()
+    # each kept result against the plain FP64 form of the same contraction
+    worst = 0.0
+    for x, C in kept:
+        c, A, a, B, b, _ = picks[x]
+        Cp, _ = ta.contract(w, c, 1.0, A, a, B, b, precision=ta.PRECISION_FP64)
+        y, z = C.download(), Cp.download()
+        worst = max(worst, float(np.linalg.norm(y - z) / max(np.linalg.norm(z), 1e-300)))
+        del Cp, C
     flops = sum(r["flops"] for r in results)
+    nrej = sum(rejected.values())
     _line(args, "served nonzero-block TFLOP/s; p50/p99 latency", flops / wall / 1e12, "TFLOP/s",
           wall * 1e3 / max(1, len(results)),
-          {"workload": f"{args.requests} Poisson requests at {args.rate}/s over block-sparse, "
-                       "ccsd-like and batched families, scales U[0.25,1] (ccsd-like <= 0.5), "
-                       "150 GB admission budget", "precision": args.precision},
+          {"workload": f"{args.requests} Poisson requests at {args.rate}/s, families "
+                       f"block-sparse/ccsd-like/batched in proportion {args.mix}, scales "
+                       "U[0.25,1] (ccsd-like at six scales over [0.25,1]), 150 GB admission "
+                       "budget, one persistent served GEMM", "precision": args.precision,
+                       "slices": args.slices},
           {"latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"], "mean": st["mean_ms"]},
            "requests_per_s": len(results) / wall, "completed": st["completed"],
-           "rejected": st["rejected"] + rejected[0], "failed": st["failed"],
-           "failures": failures, "batches": st["batches"],
-           "peak_admitted_bytes": st["peak_bytes"]})
+           "rejected": nrej, "rejected_by_kind": rejected, "failed": st["failed"],
+           "failures": failures, "kernel_waves": st["batches"],
+           "peak_admitted_bytes": st["peak_bytes"],
+           "checked_vs_plain": {"requests": len(kept), "max_rel_err": worst}})
 
 
 def main():
@@ -629,6 +672,10 @@ def main():
     ap.add_argument("--count", type=int, default=512, help="batched: contractions")
     ap.add_argument("--requests", type=int, default=300, help="serve: requests")
     ap.add_argument("--rate", type=float, default=40.0, help="serve: Poisson arrivals / s")
+    ap.add_argument("--mix", default="4,1,5",
+                    help="serve: weights of the block-sparse, ccsd-like and batched families")
+    ap.add_argument("--check", type=int, default=24,
+                    help="serve: served results checked against the plain form")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -116,7 +116,9 @@ void tagpu_threshold_set(tagpu_ctx* ctx, float threshold);
 /* ---- arrays --------------------------------------------------------------
  * hashmarks[d] holds ntiles[d]+1 increasing boundaries of dimension d
  * (TiledRange1).  rank <= 8.  A new array is dense (DensePolicy) until a
- * shape is set. */
+ * shape is set.  It holds no device memory until it is first written
+ * (upload, generate, a shape) or read; an array read before it was written
+ * holds zero tiles. */
 tagpu_status tagpu_array_create(tagpu_ctx* ctx, int rank, const int64_t* ntiles,
                                 const int64_t* const* hashmarks,
                                 tagpu_array** out);
@@ -219,7 +221,8 @@ tagpu_status tagpu_array_get_hashmarks(const tagpu_array* a, int d,
 /* ---- contraction -------------------------------------------------------- */
 typedef struct tagpu_contract_opts {
   int precision;              /* tagpu_precision */
-  int slices;                 /* Ozaki slices per operand, 2..7, 0 = default (6) */
+  int slices;                 /* Ozaki slices per operand, 2..7, 0 = default (7:
+                                 55-bit digits; 6 is faster, 47-bit) */
   float threshold;            /* result screening threshold, <0 = default */
   int autotune;               /* emulated form: time the GEMM schedules (block
                                  order, accumulation chunk) on first use of a
@@ -341,7 +344,7 @@ typedef struct tagpu_server_config {
                                  0 = no budget */
   int max_batch;              /* contractions per launch, 0 = 64 */
   int precision;              /* default precision of requests */
-  int slices;                 /* default Ozaki slices, 0 = 6 */
+  int slices;                 /* default Ozaki slices, 0 = 7 */
 } tagpu_server_config;
 typedef struct tagpu_request {
   const char* c_idx;

@@ -150,7 +150,8 @@ def test_ozaki_batch_graph(ta, world):
     world.check(L.tagpu_batch_run(bh))
     first = [o.download().copy() for o in outs]
     for (A, B), f in zip(pairs, first):
-        ref, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI)
+        ref, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI,
+                             slices=6)
         assert np.array_equal(ref.download(), f)
     world.check(L.tagpu_batch_run(bh))
     for o, f in zip(outs, first):
@@ -203,7 +204,7 @@ def test_ozaki_autotune_identical_and_cached(ta, world, tmp_path, monkeypatch):
                          autotune=True)
     assert np.array_equal(got.download(), ref.download())
     lines = cache.read_text().split("\n")
-    assert lines[0].startswith("S6_") and len(lines[0].split()) == 4
+    assert lines[0].startswith("S7_") and len(lines[0].split()) == 4
     again, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI,
                            autotune=True)
     assert np.array_equal(again.download(), ref.download())

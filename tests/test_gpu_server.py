@@ -81,6 +81,23 @@ def test_server_rejects_by_footprint(ta, world):
     assert st["rejected"] == 1 and st["submitted"] == 1
 
 
+def test_unwritten_array_holds_no_storage(ta, world):
+    """An array is only given device memory when written or read: a 4-index
+    operand of 400^4 elements (205 GB stored, 358 GB of digit bricks) is
+    created without allocating, refused by admission, and a small unwritten
+    array reads as zero tiles."""
+    hv, ho = list(range(0, 401, 50)), [0, 16, 32]
+    V = ta.DistArray(world, ta.TiledRange([hv, hv, hv, hv]))
+    T = ta.DistArray(world, ta.TiledRange([hv, hv, ho, ho]))
+    srv = ta.Server(world, hbm_budget_bytes=150 << 30)
+    with pytest.raises(ta.TAGPUError) as e:
+        srv.submit("a,b,i,j", 1.0, V, "a,b,c,d", T, "c,d,i,j", precision=ta.PRECISION_OZAKI)
+    assert e.value.status == 6
+    srv.stop()
+    small = ta.DistArray(world, ta.TiledRange([[0, 30, 70], [0, 50]]))
+    assert np.array_equal(small.download(), np.zeros(70 * 50))
+
+
 def test_server_concurrent_submitters(ta, world):
     reqs = make_requests(ta, world, 9, seed=3)
     alone = [ta.contract(world, c, al, A, a, B, b, precision=p)[0].download()

@@ -632,7 +632,7 @@ class Server:
     """Request loop: HBM-footprint admission and continuous batching."""
 
     def __init__(self, world: World, hbm_budget_bytes=0, max_batch=64,
-                 precision=PRECISION_FP64, slices=6):
+                 precision=PRECISION_FP64, slices=7):
         self.world = world
         cfg = ServerConfig(hbm_budget_bytes, max_batch, precision, slices)
         h = _vp()

@@ -12,6 +12,28 @@
 
 namespace tagpu {
 
+// cudaMallocAsync from the device's default pool.  The pool keeps freed
+// blocks (release threshold: never), and under a mix of very large and small
+// requests its free memory can be too fragmented for a large block; on
+// failure the stream's pending frees are waited for, the pool's unused memory
+// is returned to the device and the allocation is tried once more.
+inline cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s) {
+  cudaError_t e = cudaMallocAsync(p, bytes, s);
+  if (e == cudaSuccess) return e;
+  cudaGetLastError();
+  int dev = 0;
+  cudaMemPool_t pool;
+  if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return e;
+  }
+  cudaMemPoolTrimTo(pool, 0);
+  e = cudaMallocAsync(p, bytes, s);
+  if (e != cudaSuccess) cudaGetLastError();
+  return e;
+}
+
 // Kernel launches made by this library (every launch site counts itself).
 void count_launch();
 int64_t launch_count();

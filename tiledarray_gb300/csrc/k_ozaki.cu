@@ -1868,9 +1868,8 @@ struct OzakiPlan {
   tagpu_status alloc(T** p, size_t n, std::string* e) {
     void* q = nullptr;
     const size_t bytes_ = std::max<size_t>(1, n) * sizeof(T);
-    cudaError_t ce = cudaMallocAsync(&q, bytes_, s);
+    cudaError_t ce = pool_alloc(&q, bytes_, s);
     if (ce != cudaSuccess) {
-      cudaGetLastError();
       *e = std::string("ozaki scratch allocation failed: ") + cudaGetErrorString(ce);
       return TAGPU_ERR_NOMEM;
     }

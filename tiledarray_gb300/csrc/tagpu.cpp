@@ -121,9 +121,8 @@ tagpu_status dev_alloc(tagpu_ctx* ctx, void** p, size_t bytes) {
   if (ctx->budget && ctx->used.load() + bytes > ctx->budget)
     return fail(ctx, TAGPU_ERR_NOMEM, "device budget exceeded: %zu + %zu > %zu bytes",
                 ctx->used.load(), bytes, ctx->budget);
-  cudaError_t e = cudaMallocAsync(p, bytes, ctx->stream);
+  cudaError_t e = pool_alloc(p, bytes, ctx->stream);
   if (e != cudaSuccess) {
-    cudaGetLastError();
     return fail(ctx, TAGPU_ERR_NOMEM, "cudaMallocAsync(%zu) failed: %s", bytes,
                 cudaGetErrorString(e));
   }
@@ -277,6 +276,20 @@ tagpu_status ensure_storage(tagpu_array* a) {
   if (st) return st;
   a->data = static_cast<double*>(p);
   a->bytes = need;
+  return TAGPU_OK;
+}
+
+// An array made by tagpu_array_create holds no device memory until it is
+// written (upload, generate, a shape, a contraction result) or read; a read of
+// an array never written sees zero tiles, like a TiledArray DistArray whose
+// tiles were initialised to zero.  So an operand too large for the device can
+// still be described (and a request naming it refused by admission).
+tagpu_status materialize(const tagpu_array* ca) {
+  tagpu_array* a = const_cast<tagpu_array*>(ca);
+  if (a->data || a->elements == 0) return TAGPU_OK;
+  tagpu_status st = ensure_storage(a);
+  if (st) return st;
+  CUDA_TRY(a->ctx, cudaMemsetAsync(a->data, 0, a->bytes, a->ctx->stream));
   return TAGPU_OK;
 }
 
@@ -607,10 +620,7 @@ tagpu_status tagpu_array_create(tagpu_ctx* ctx, int rank, const int64_t* ntiles,
   }
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   cudaSetDevice(ctx->device);
-  std::unique_ptr<tagpu_array> a(new_array(ctx, hm));
-  tagpu_status st = ensure_storage(a.get());
-  if (st) return st;
-  *out = a.release();
+  *out = new_array(ctx, hm);   // storage on first write or read
   return TAGPU_OK;
 }
 
@@ -686,6 +696,7 @@ tagpu_status tagpu_array_download(const tagpu_array* a, double* tiles, int64_t n
     return fail(ctx, TAGPU_ERR_INVALID, "download: buffer holds %lld elements, array %lld",
                 (long long)n, (long long)a->elements);
   if (n && !tiles) return fail(ctx, TAGPU_ERR_INVALID, "download: null buffer");
+  if (tagpu_status st = materialize(a)) return st;
   if (n) {
     if (link_copy_usable(tiles))
       launch_link_copy(ctx->stream, tiles, a->data, n * sizeof(double));
@@ -836,6 +847,7 @@ tagpu_status tagpu_array_truncate(tagpu_array* a, float threshold) {
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   if (a->dense) return TAGPU_OK;   // DensePolicy: no-op
   cudaSetDevice(ctx->device);
+  if (tagpu_status st = materialize(a)) return st;
   const float thr = threshold < 0 ? ctx->threshold : threshold;
   const int64_t n = a->ntiles();
   std::vector<int64_t> present, offs(1, 0);
@@ -914,6 +926,7 @@ tagpu_status tagpu_array_get_tile(const tagpu_array* a, int64_t ordinal, double*
                 (long long)n, (long long)vol);
   if (n && !tile) return fail(ctx, TAGPU_ERR_INVALID, "get_tile: null buffer");
   cudaSetDevice(ctx->device);
+  if (tagpu_status st = materialize(a)) return st;
   if (n)
     CUDA_TRY(ctx, cudaMemcpyAsync(tile, a->data + a->off[ordinal], n * sizeof(double),
                                   cudaMemcpyDeviceToHost, ctx->stream));
@@ -1038,6 +1051,7 @@ tagpu_status tagpu_array_save(const tagpu_array* a, const char* path) {
   tagpu_ctx* ctx = a->ctx;
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   cudaSetDevice(ctx->device);
+  if (tagpu_status st = materialize(a)) return st;
   File out(path, "wb");
   if (!out.f) return fail(ctx, TAGPU_ERR_INVALID, "save: cannot open %s", path);
   PinnedStage stage;
@@ -1224,6 +1238,7 @@ tagpu_status tagpu_array_serialize(const tagpu_array* a, const char* path,
   tagpu_ctx* ctx = a->ctx;
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   cudaSetDevice(ctx->device);
+  if (tagpu_status st = materialize(a)) return st;
   File out(path, "wb");
   if (!out.f) return fail(ctx, TAGPU_ERR_INVALID, "serialize: cannot open %s", path);
   PinnedStage stage;
@@ -1515,7 +1530,7 @@ struct Contraction {
   bool dense = false;
   double alpha = 1.0;
   int precision = TAGPU_PRECISION_FP64;
-  int slices = 6;
+  int slices = 7;
   // operands in GEMM order
   tagpu_array* Aop = nullptr;
   tagpu_array* Bop = nullptr;
@@ -1830,6 +1845,7 @@ tagpu_status run_shape_and_pairs(Contraction& c) {
 tagpu_status prepare_operands(Contraction& c, tagpu_array* A, tagpu_array* B) {
   tagpu_ctx* ctx = c.ctx;
   tagpu_status e;
+  if ((e = materialize(A)) || (e = materialize(B))) return e;
   auto explicit_permute = [&](tagpu_array* X, const std::vector<int>& perm,
                               std::unique_ptr<tagpu_array>& own) -> tagpu_status {
     own.reset(permuted_layout(X, perm));
@@ -1994,7 +2010,7 @@ tagpu_status plan_all(Contraction& c, const char* c_idx, double alpha, tagpu_arr
                       const tagpu_contract_opts* opts) {
   tagpu_ctx* ctx = c.ctx;
   c.precision = opts ? opts->precision : TAGPU_PRECISION_FP64;
-  c.slices = opts && opts->slices > 0 ? opts->slices : 6;
+  c.slices = opts && opts->slices > 0 ? opts->slices : 7;
   const float cthr = opts && opts->threshold >= 0 ? opts->threshold : ctx->threshold;
   if (c.precision != TAGPU_PRECISION_FP64 && c.precision != TAGPU_PRECISION_OZAKI)
     return fail(ctx, TAGPU_ERR_INVALID, "unknown precision %d", c.precision);
@@ -2333,6 +2349,7 @@ tagpu_status tagpu_contract_accumulate(tagpu_ctx* ctx, const char* c_idx, double
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   cudaSetDevice(ctx->device);
   tagpu_array* p = nullptr;
+  if (tagpu_status st = materialize(C)) return st;
   tagpu_status st = contract_impl(ctx, c_idx, alpha, A, a_idx, B, b_idx, opts, &p, &ctx->last);
   if (st) return st;
   std::unique_ptr<tagpu_array> P(p);
@@ -2726,7 +2743,7 @@ size_t footprint_bound(tagpu_array* A, const std::vector<std::string>& ai, tagpu
   bytes += mt * nt * kt * 4 + mt * nt * 32;       // pair list, offsets
   bytes += (double)A->bytes + (double)B->bytes;   // explicit permutations
   if (o.precision == TAGPU_PRECISION_OZAKI) {
-    const int S = o.slices > 0 ? o.slices : 6;
+    const int S = o.slices > 0 ? o.slices : 7;
     const double kk = std::ceil(k / 32.0) * 32.0;
     bytes += (std::ceil(m / 128.0) * 128.0 + std::ceil(n / 64.0) * 64.0) * kk * 2.0 * S;
     bytes += (m + n) * 24 + (m / 128.0 + n / 64.0 + 2) * (k / 32.0 + 1) * 32;
@@ -2977,7 +2994,7 @@ tagpu_status tagpu_server_start(tagpu_ctx* ctx, const tagpu_server_config* cfg,
   auto* s = new tagpu_server;
   s->ctx = ctx;
   if (cfg) s->cfg = *cfg;
-  if (s->cfg.slices <= 0) s->cfg.slices = 6;
+  if (s->cfg.slices <= 0) s->cfg.slices = 7;
   cudaSetDevice(ctx->device);
   if (cudaStreamCreateWithFlags(&s->gemm_stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete s;
