@@ -1099,26 +1099,46 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
       }
       if (!ok) break;
       // recombination: C = alpha * 2^(E_A + E_B - 8 M) * (hi * 2^(8(TOP-5)) + lo) * u_TOP,
-      // exact integer to correctly rounded double, then one multiply by alpha
-      const int64_t gr = (int64_t)rb * BM + rloc;
-      if (gr < P.M_total) {
-        const int ti = P.row_tile[gr], lr = P.row_local[gr], ea = P.EA[gr];
-        const int base = (int)((uint32_t)P.unitM[2 * b + rank] & 0x0FFFFFFFu);
-        const bool unit_alpha = P.alpha == 1.0;
+      // exact integer to correctly rounded double, then one multiply by alpha.
+      // The column data of the warp's 32 columns is loaded one column per
+      // lane and broadcast by shuffles, the row's per thread, and the tile
+      // offset once per result tile crossed: every load is issued before the
+      // first store, so the stores do not serialise reloads behind them.
+      {
+        const uint32_t full = 0xffffffffu;
+        const int64_t gcl = (int64_t)cb * BN + half * 32 + lane;
+        const bool cok = gcl < P.N_total;
+        const int tj_l = cok ? P.col_tile[gcl] : -1;
+        const int cl_l = cok ? P.col_local[gcl] : 0;
+        const int eb_l = cok ? P.EB[gcl] - 1022 : 0;
+        const int64_t gr = (int64_t)rb * BM + rloc;
+        const bool rok = gr < P.M_total;
+        const int ti = rok ? P.row_tile[gr] : 0;
+        const int64_t mrow = rok ? P.hel * P.msz[ti] + P.row_local[gr] : 0;
+        const int e2 = (2 - 8 * TOP) + (rok ? P.EA[gr] - 1022 : 0) -
+                       8 * (int)((uint32_t)P.unitM[2 * b + rank] & 0x0FFFFFFFu);
+        const int64_t* __restrict__ coff = P.coff + (int64_t)ti * P.Nt;
+        const int* __restrict__ nsz = P.nsz;
+        double* __restrict__ const Cout = P.C;
+        const double alpha = P.alpha;
+        int tj_prev = -1;
+        double* dst = nullptr;   // this row's element of the current tile's first column
+        int j0 = 0;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
-          const int64_t gc = (int64_t)cb * BN + half * 32 + j;
-          if (gc < P.N_total) {
-            const int tj = P.col_tile[gc];
-            const int64_t off = P.coff[(int64_t)ti * P.Nt + tj];
-            if (off >= 0) {
-              const double v =
-                  exact_to_double(hi[j], lo[j], 8 * (TOP - kExactTop),
-                                  (2 - 8 * TOP) + (ea - 1022) + (P.EB[gc] - 1022) - 8 * base);
-              const int64_t nn = P.nsz[tj];
-              P.C[off + (P.hel * P.msz[ti] + lr) * nn + P.col_local[gc]] =
-                  unit_alpha ? v : P.alpha * v;
-            }
+          const int tj = __shfl_sync(full, tj_l, j);
+          const int eb = __shfl_sync(full, eb_l, j);
+          if (tj < 0) break;   // past the last column: so are the rest (warp-uniform)
+          if (tj != tj_prev) {   // a new result tile (warp-uniform)
+            const int cl = __shfl_sync(full, cl_l, j);
+            const int64_t off = rok ? coff[tj] : -1;
+            dst = off >= 0 ? Cout + off + mrow * (int64_t)nsz[tj] + cl : nullptr;
+            tj_prev = tj;
+            j0 = j;
+          }
+          if (dst) {
+            const double v = exact_to_double(hi[j], lo[j], 8 * (TOP - kExactTop), e2 + eb);
+            dst[j - j0] = alpha == 1.0 ? v : alpha * v;
           }
         }
       }
@@ -1205,8 +1225,8 @@ __global__ void shift_kernel(const OzParams* __restrict__ views, const int64_t* 
       T[c] = min(T[c], __shfl_xor_sync(0xffffffffu, T[c], o));
     }
   int E[2];
-#pragma unroll
   const int emax = min(2, 9 - (S + 1));   // levels 2..9 fill the tensor memory
+#pragma unroll
   for (int c = 0; c < 2; ++c) E[c] = M[c] >= kNoShift ? 0 : min(emax, (T[c] - 8 * M[c] + 3) >> 3);
   unsigned long long prod = 0;
   for (int64_t x = x0 + lane; x < x1; x += 32) {

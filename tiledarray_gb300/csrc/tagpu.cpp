@@ -2761,11 +2761,13 @@ size_t footprint_bound(tagpu_array* A, const std::vector<std::string>& ai, tagpu
 // finishes its current unit.  A request completes when all its jobs are
 // counted done (and its post-permutation, if any, has run).  Other requests
 // (plain FP64, emulated plans built in row chunks or with another slice
-// count) run on the context's stream at once; they share the GPU with the
-// served kernel, which leaves a few clusters free for them and for the
-// preparation kernels.
+// count) run alone on the whole GPU: publication pauses, the served jobs out
+// finish, the served kernel stops, and they run on the context's stream one
+// after another; then publication resumes.  (Run beside the served kernel,
+// they would get only the few clusters it leaves free for the preparation
+// kernels.)
 void tagpu_server::run() {
-  std::deque<std::shared_ptr<Req>> prepping, serving;
+  std::deque<std::shared_ptr<Req>> prepping, serving, exclusive;
   LaunchBufs lb(ctx);
   const int S = cfg.slices;
   // jobs of at most this many (unit, k block) stages go to the first lane:
@@ -2809,7 +2811,7 @@ void tagpu_server::run() {
     std::vector<std::shared_ptr<Req>> batch;
     {
       std::unique_lock<std::mutex> lk(m);
-      const bool busy = !prepping.empty() || !serving.empty();
+      const bool busy = !prepping.empty() || !serving.empty() || !exclusive.empty();
       if (!busy) {
         cv.wait(lk, [&] { return stopping || !queue.empty(); });
         if (stopping && queue.empty()) break;
@@ -2874,8 +2876,32 @@ void tagpu_server::run() {
             cudaGetLastError();
             e = TAGPU_ERR_CUDA;
           }
-        } else if (!e) {
-          // not served: its own launches on the context's stream, now
+        }
+      }
+      if (e) {
+        finish(r, e);
+        continue;
+      }
+      if (!servable) {
+        exclusive.push_back(r);   // runs alone once the served jobs out are done
+        continue;
+      }
+      prepping.push_back(r);
+    }
+    // requests that run alone: once no served job is out
+    if (!exclusive.empty() && serving.empty()) {
+      if (served) {
+        std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+        ozaki_serve_reset(served, &err);   // stops the served kernel
+      }
+      while (!exclusive.empty()) {
+        auto r = exclusive.front();
+        exclusive.pop_front();
+        tagpu_status e;
+        {
+          std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+          cudaSetDevice(ctx->device);
+          Contraction& c = *r->plan;
           std::vector<Contraction*> one{&c};
           e = enqueue_gemms(ctx, one, lb, true, ctx->stream);
           if (!e && c.post) c.post->enqueue(ctx->stream, c.post_in, c.post_out);
@@ -2884,20 +2910,17 @@ void tagpu_server::run() {
             e = TAGPU_ERR_CUDA;
           }
           if (!e && lb.any_error()) e = TAGPU_ERR_TIMEOUT;
-          ++batches;
-          r->res.batch_size = 1;
-          r->res.batch_id = next_batch++;
         }
-      }
-      if (e || !servable) {
+        ++batches;
+        r->res.batch_size = 1;
+        r->res.batch_id = next_batch++;
         finish(r, e);
-        continue;
       }
-      prepping.push_back(r);
     }
-    // publish the requests whose preparation has finished (in admission order)
+    // publish the requests whose preparation has finished (in admission
+    // order), unless requests wait to run alone
     bool published = false;
-    while (!prepping.empty()) {
+    while (!prepping.empty() && exclusive.empty()) {
       auto& r = prepping.front();
       const cudaError_t q = cudaEventQuery(r->prep);
       if (q == cudaErrorNotReady) break;
