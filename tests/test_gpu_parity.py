@@ -255,6 +255,39 @@ def test_truncate_matches_make_array(oracle, ta, world):
     assert info.zero_tiles == nt * nt - len(got)
 
 
+def test_tile_norms_at_float_ties(oracle, ta, world):
+    """Device tile norms equal the sequential-order norms bit for bit, also for
+    tiles whose sum of squares sits at a float rounding boundary of the norm
+    (where the kernel's error bound cannot decide and it sums in order), and
+    for large tiles."""
+    rng = np.random.default_rng(3)
+    f = rng.uniform(1.0, 2.0, 48).astype(np.float32)
+    f_next = np.nextafter(f, np.float32(np.inf))
+    mids = (f.astype(np.float64) + f_next.astype(np.float64)) / 2   # halfway between floats
+    tiles = []
+    for x, m in enumerate(mids):
+        kind = x % 4
+        if kind == 0:
+            t = np.array([m])                          # one element, at the tie
+        elif kind == 1:
+            t = np.full(100, m / 10.0)                 # equal elements, squares summing near m^2
+        elif kind == 2:
+            t = rng.uniform(-1.0, 1.0, 5000)
+            t *= m / np.sqrt(np.sum(t * t))            # sum of squares near m^2
+        else:
+            t = rng.uniform(-1.0, 1.0, int(rng.integers(1, 70000)))
+        tiles.append(t)
+    h = [0] + np.cumsum([len(t) for t in tiles]).tolist()
+    n = len(tiles)
+    A = ta.DistArray(world, ta.TiledRange([h]), norms=np.ones(n, np.float32), do_not_scale=True,
+                     threshold=0.0)
+    A.upload(np.concatenate(tiles))
+    A.truncate(0.0)   # the norms again, from the device data
+    raw = np.asarray([oracle.tile_norm(t) for t in tiles], np.float32)
+    want, _ = oracle.scale_norms(oracle.TiledRange([h]), raw, 0.0)
+    assert np.array_equal(A.norms(), want.ravel())
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_contract_accumulate(ta, world, precision):
     """C("i,j") += alpha * A2("i,k") * B2("k,j"): the shape is the float sum of

@@ -8,9 +8,10 @@
 //
 // Norms: Tensor::norm (tensor/tensor.h:3768-3787) is sqrt of a sequential
 // double sum of x*x in storage order (math/vector_op.h:561-577), stored as
-// float.  One thread walks one tile in that order, rounding every product and
-// sum separately, so the norms (and the SparseShape built from them) match
-// the host bit for bit.
+// float.  A warp per tile estimates the sum and proves from an error bound
+// which float the sequential sum rounds to, walking the tile in that order
+// itself only when the bound cannot decide (tile_norms_kernel), so the norms
+// (and the SparseShape built from them) match the host bit for bit.
 #include <cuda_runtime.h>
 
 #include "internal.h"
@@ -62,15 +63,63 @@ __global__ void generate_kernel(GenDesc g, int64_t ntiles,
   }
 }
 
+// Tile norms, bit-exact with the sequential order of the reference's serial
+// reduction (math/vector_op.h:561-577 reduce_op_serial, used by Tensor::norm):
+// s = fl(s + fl(x_i * x_i)) for i = 0..n-1, then float(sqrt(s)).
+//
+// One warp per tile.  The lanes sum fma(x, x, .) over a strided share of the
+// tile (coalesced), giving an estimate S of the exact sum of squares with
+// relative error at most gamma(n/32 + 5), gamma(m) = m u / (1 - m u),
+// u = 2^-53.  The sequential sum differs from the exact one by at most
+// gamma(n) of it (recursive summation of n rounded products, Higham,
+// "Accuracy and Stability of Numerical Algorithms", 4.2), plus n * 2^-1074
+// absolute where products fall below the normal range.  If both ends of
+// that interval around S give the same float after the correctly rounded
+// square root and the rounding to float (both monotonic), the sequential
+// result gives it too; otherwise lane 0 runs the sequential loop itself.
+// The fallback is rare: the interval is about n * 2^-52 wide relative to S
+// against float spacing 2^-23, so a tile of n elements takes it with
+// probability about n * 2^-29.
 __global__ void tile_norms_kernel(int64_t ntiles, const int64_t* __restrict__ tile_off,
                                   const double* __restrict__ data, float* __restrict__ norms) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (t >= ntiles) return;
   const double* x = data + tile_off[t];
   const int64_t n = tile_off[t + 1] - tile_off[t];
-  double s = 0.0;
-  for (int64_t i = 0; i < n; ++i) s = __dadd_rn(s, __dmul_rn(x[i], x[i]));
-  norms[t] = __double2float_rn(__dsqrt_rn(s));
+  double a0 = 0.0, a1 = 0.0;
+  int64_t i = lane;
+  for (; i + 32 < n; i += 64) {
+    const double u0 = x[i], u1 = x[i + 32];
+    a0 = fma(u0, u0, a0);
+    a1 = fma(u1, u1, a1);
+  }
+  if (i < n) a0 = fma(x[i], x[i], a0);
+  double est = a0 + a1;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) est += __shfl_xor_sync(0xffffffffu, est, o);
+  float out = 0.0f;
+  bool exact = false;
+  if (lane == 0) {
+    const double u = 0x1.0p-53;
+    const double m_est = (double)(n / 64 + 8), m_seq = (double)n + 2.0;
+    // plus 4u for the roundings of the two ends themselves
+    const double g = (m_seq + m_est) * u / (1.0 - (m_seq + m_est) * u) + 4.0 * u;
+    const double tiny = ((double)n + 2.0) * 0x1.0p-1074 * 4.0;
+    const double lo = est * (1.0 - g) - tiny, hi = est * (1.0 + g) + tiny;
+    const float flo = __double2float_rn(__dsqrt_rn(lo > 0.0 ? lo : 0.0));
+    const float fhi = __double2float_rn(__dsqrt_rn(hi));
+    exact = flo == fhi && est == est && est < 1.0e300;
+    out = flo;
+  }
+  exact = __shfl_sync(0xffffffffu, exact ? 1 : 0, 0) != 0;
+  if (lane != 0) return;
+  if (!exact) {
+    double s = 0.0;
+    for (int64_t k = 0; k < n; ++k) s = __dadd_rn(s, __dmul_rn(x[k], x[k]));
+    out = __double2float_rn(__dsqrt_rn(s));
+  }
+  norms[t] = out;
 }
 
 }  // namespace
@@ -90,8 +139,8 @@ void launch_generate(cudaStream_t s, const GenDesc& g, int64_t ntiles,
 void launch_tile_norms(cudaStream_t s, int64_t ntiles, const int64_t* tile_off,
                        const double* data, float* norms) {
   if (ntiles <= 0) return;
-  const int threads = 64;
-  tile_norms_kernel<<<(unsigned)((ntiles + threads - 1) / threads), threads, 0, s>>>(
+  const int threads = 256;   // eight tiles per block, a warp each
+  tile_norms_kernel<<<(unsigned)((ntiles * 32 + threads - 1) / threads), threads, 0, s>>>(
       ntiles, tile_off, data, norms);
   count_launch();
 }

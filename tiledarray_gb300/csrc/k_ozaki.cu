@@ -242,45 +242,40 @@ __host__ __device__ constexpr uint32_t idesc_n(int n) {
 // FP64 arithmetic on this GPU is far slower than integer arithmetic.  The
 // rare results outside the normal range take the FP64 library route.
 __device__ __forceinline__ double exact_to_double(int64_t hi, int64_t lo, int sh, int e2) {
-  // 128-bit two's complement W = hi * 2^sh + lo
-  uint64_t wl = (uint64_t)hi << sh;
-  int64_t wh = sh ? (hi >> (64 - sh)) : (hi < 0 ? -1 : 0);
-  const uint64_t lo_u = (uint64_t)lo;
-  const uint64_t sum = wl + lo_u;
-  wh += (int64_t)(lo < 0 ? -1 : 0) + (sum < wl ? 1 : 0);
-  wl = sum;
+  // W = hi * 2^sh + lo as a 128-bit two's complement wh:wl
+  const uint64_t hl = (uint64_t)hi << sh;
+  int64_t wh = sh ? (hi >> (64 - sh)) : (hi >> 63);
+  const uint64_t wl = hl + (uint64_t)lo;
+  wh += (lo >> 63) + (int64_t)(wl < hl);
   const bool neg = wh < 0;
-  uint64_t mh = (uint64_t)wh, ml = wl;
-  if (neg) {  // magnitude
+  uint64_t mh = (uint64_t)wh, ml = wl;   // |W|
+  if (neg) {
     ml = ~ml + 1;
     mh = ~mh + (ml == 0 ? 1 : 0);
   }
-  if (mh == 0 && ml == 0) return 0.0;
-  const int lz = mh ? __clzll((long long)mh) : 64 + __clzll((long long)ml);
-  const int p = 127 - lz;                // position of the leading one
-  uint64_t mant;
-  if (p <= 52) {
-    mant = ml << (52 - p);
+  // top: the 64 bits from the leading one down; sticky: any one below them;
+  // p: position of the leading one in W
+  uint64_t top;
+  bool sticky;
+  int p;
+  if (mh) {
+    const int lz = __clzll((long long)mh);
+    top = lz ? (mh << lz) | (ml >> (64 - lz)) : mh;
+    sticky = (lz ? (ml << lz) : ml) != 0;
+    p = 127 - lz;
   } else {
-    const int r = p - 52;                // bits dropped
-    // mantissa = W >> r, remainder bits for rounding
-    uint64_t q, rem_hi_bit, sticky;
-    if (r < 64) {
-      q = (ml >> r) | (r ? (mh << (64 - r)) : 0);
-      rem_hi_bit = (ml >> (r - 1)) & 1;
-      sticky = (r >= 2) ? (ml & ((1ull << (r - 1)) - 1)) : 0;
-    } else {
-      const int r2 = r - 64;
-      q = mh >> r2;
-      rem_hi_bit = r2 ? ((mh >> (r2 - 1)) & 1) : (ml >> 63);
-      sticky = (r2 >= 2 ? (mh & ((1ull << (r2 - 1)) - 1)) : 0) |
-               (r2 ? ml : (ml & ((1ull << 63) - 1)));
-    }
-    mant = q;
-    if (rem_hi_bit && (sticky || (mant & 1))) ++mant;
+    if (!ml) return 0.0;
+    const int lz = __clzll((long long)ml);
+    top = ml << lz;
+    sticky = false;
+    p = 63 - lz;
   }
-  int ex = p + e2;                       // value = mant * 2^(ex - 52)
-  if (mant >> 53) {                      // rounding carried into a new bit
+  // round to 53 bits, nearest even
+  uint64_t mant = top >> 11;
+  const uint64_t rem = top & 0x7FF;
+  mant += (rem > 0x400 || (rem == 0x400 && (sticky || (mant & 1)))) ? 1 : 0;
+  int ex = p + e2;   // value = mant * 2^(ex - 52)
+  if (mant >> 53) {  // rounding carried into a new bit
     mant >>= 1;
     ++ex;
   }
@@ -331,11 +326,16 @@ struct OzParams {
   int* err;                  // error flag (0 = ok)
 };
 
+// Epilogue staging: per epilogue warp, 32 rows x 16 columns of results
+// (row stride 17 doubles: the row-per-lane writes and the column-per-lane
+// reads both hit 32 distinct banks pairs).
+constexpr int EPI_LD = 17;
+constexpr int EPI_BYTES = EPI_WARPS * 32 * EPI_LD * 8;   // 34,816
 template <int S>
 struct Smem {
   static constexpr int kStages = (S * (A_SLICE_BYTES + B_SLICE_BYTES) * 3 <= 200 * 1024) ? 3 : 2;
   static constexpr int kStageBytes = S * (A_SLICE_BYTES + B_SLICE_BYTES);
-  static constexpr int kBytes = kStages * kStageBytes + 1024;
+  static constexpr int kBytes = kStages * kStageBytes + EPI_BYTES + 1024;
 };
 
 // ---------------------------------------------------------------------------
@@ -1111,35 +1111,53 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
         const int tj_l = cok ? P.col_tile[gcl] : -1;
         const int cl_l = cok ? P.col_local[gcl] : 0;
         const int eb_l = cok ? P.EB[gcl] - 1022 : 0;
+        const int nn_l = cok ? P.nsz[tj_l] : 0;
         const int64_t gr = (int64_t)rb * BM + rloc;
         const bool rok = gr < P.M_total;
-        const int ti = rok ? P.row_tile[gr] : 0;
-        const int64_t mrow = rok ? P.hel * P.msz[ti] + P.row_local[gr] : 0;
+        const int ti_l = rok ? P.row_tile[gr] : -1;
+        const int64_t mrow_l = rok ? P.hel * P.msz[ti_l] + P.row_local[gr] : 0;
         const int e2 = (2 - 8 * TOP) + (rok ? P.EA[gr] - 1022 : 0) -
                        8 * (int)((uint32_t)P.unitM[2 * b + rank] & 0x0FFFFFFFu);
-        const int64_t* __restrict__ coff = P.coff + (int64_t)ti * P.Nt;
-        const int* __restrict__ nsz = P.nsz;
+        const int64_t* __restrict__ coff = P.coff;
+        const int64_t Nt = P.Nt;
         double* __restrict__ const Cout = P.C;
         const double alpha = P.alpha;
-        int tj_prev = -1;
-        double* dst = nullptr;   // this row's element of the current tile's first column
-        int j0 = 0;
+        double* sb = reinterpret_cast<double*>(stage_base + STAGES * STAGE_BYTES) +
+                     (warp - 2) * 32 * EPI_LD;
+        // Two passes of 16 columns: each lane converts its row's values into
+        // the warp's staging rows, then the warp writes them out with lane
+        // = column (lanes 0-15 one row, 16-31 the next), so every store
+        // instruction writes two 128-byte row segments.
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int tj = __shfl_sync(full, tj_l, j);
-          const int eb = __shfl_sync(full, eb_l, j);
-          if (tj < 0) break;   // past the last column: so are the rest (warp-uniform)
-          if (tj != tj_prev) {   // a new result tile (warp-uniform)
-            const int cl = __shfl_sync(full, cl_l, j);
-            const int64_t off = rok ? coff[tj] : -1;
-            dst = off >= 0 ? Cout + off + mrow * (int64_t)nsz[tj] + cl : nullptr;
-            tj_prev = tj;
-            j0 = j;
-          }
-          if (dst) {
+        for (int hc = 0; hc < 2; ++hc) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const int j = 16 * hc + c;
+            const int eb = __shfl_sync(full, eb_l, j);
             const double v = exact_to_double(hi[j], lo[j], 8 * (TOP - kExactTop), e2 + eb);
-            dst[j - j0] = alpha == 1.0 ? v : alpha * v;
+            sb[lane * EPI_LD + c] = alpha == 1.0 ? v : alpha * v;
           }
+          __syncwarp();
+          const int c = lane & 15;
+          const int tj = __shfl_sync(full, tj_l, 16 * hc + c);
+          const int cl = __shfl_sync(full, cl_l, 16 * hc + c);
+          const int64_t nn = __shfl_sync(full, nn_l, 16 * hc + c);
+          int ti_prev = -1;
+          int64_t off = -1;
+#pragma unroll 4
+          for (int i = 0; i < 16; ++i) {
+            const int r = 2 * i + (lane >> 4);
+            const int ti = __shfl_sync(full, ti_l, r);
+            const int64_t mrow = __shfl_sync(full, mrow_l, r);
+            if (ti >= 0 && tj >= 0) {
+              if (ti != ti_prev) {
+                off = coff[(int64_t)ti * Nt + tj];
+                ti_prev = ti;
+              }
+              if (off >= 0) Cout[off + mrow * nn + cl] = sb[r * EPI_LD + c];
+            }
+          }
+          __syncwarp();
         }
       }
 #pragma unroll
