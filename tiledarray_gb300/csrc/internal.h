@@ -145,7 +145,7 @@ struct WorkItem {
   int16_t rb, cb;     // 64-row / 64-column block within the tile
 };
 void launch_dmma_gemm(cudaStream_t s, const GemmView* views, const WorkItem* items,
-                      int64_t nitems, int sm_count);
+                      int64_t nitems, int* err, unsigned long long wait_ns, int sm_count);
 
 // (d) emulated FP64 (Ozaki scheme, bf16 digit slices on tcgen05).
 // ozaki_plan sizes and fills the scratch (index maps, brick maps, block

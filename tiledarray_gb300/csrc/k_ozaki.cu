@@ -493,30 +493,33 @@ __device__ __forceinline__ void slices_full(uint32_t tmem, uint64_t ad0, uint64_
     }
   }
 }
-// Levels lo..hi of slice 1, k step 0 (B slices from lo - 1 - SH).
+// Levels lo..hi of slice p, k step ks (B slices from lo - p - SH).
 template <int S, int SH>
-__device__ __forceinline__ void slice1_run(uint32_t tmem, uint64_t ad0, uint64_t bd0, int lo,
-                                           int hi, uint32_t acc) {
+__device__ __forceinline__ void slice_run(uint32_t tmem, uint64_t ad0, uint64_t bd0, int p, int ks,
+                                          int lo, int hi, uint32_t acc) {
   if (hi < lo) return;
-  const uint64_t bd = bd0 + (uint64_t)(((lo - 2 - SH) * B_SLICE_BYTES) >> 4);
+  const uint64_t ad = ad0 + (uint64_t)((((p - 1) * A_SLICE_BYTES) >> 4) + ks * 16);
+  const uint64_t bd = bd0 + (uint64_t)((((lo - 1 - p - SH) * B_SLICE_BYTES) >> 4) + ks * 16);
   const uint32_t d = tmem + (lo - 2) * BN;
   const int nn = (hi - lo + 1) * BN;
   if (nn <= 256) {
-    tc_mma(d, ad0, bd, idesc_n(nn), acc);
+    tc_mma(d, ad, bd, idesc_n(nn), acc);
   } else {
     const int h = nn / 2;
-    tc_mma(d, ad0, bd, idesc_n(h), acc);
-    tc_mma(d + h, ad0, bd + (uint64_t)(((h / 8) * 512) >> 4), idesc_n(h), acc);
+    tc_mma(d, ad, bd, idesc_n(h), acc);
+    tc_mma(d + h, ad, bd + (uint64_t)(((h / 8) * 512) >> 4), idesc_n(h), acc);
   }
 }
 // The three stage programs, for a stage with no fresh level among its own:
 //   kStageAll:     every slice (k step 0, then 1);
-//   kStageRestartA: at a stage restarting levels zlo..5, the slices whose
-//                  lowest level lies above 5 (issued before the wait);
+//   kStageRestartA: at a stage restarting levels zlo..5, every product on a
+//                  level above 5 (each slice's run from level 6 up), issued
+//                  before the wait: about two thirds of the stage's work
+//                  covers the epilogue's reads of the restarting levels;
 //   kStageRestartC: the rest once levels zlo..5 are free and marked fresh:
-//                  slice 1's k step 0 in three runs, the restarting run
-//                  [max(zlo, 2+SH), 5] with accumulate off, then the
-//                  remaining slices below level 6.
+//                  slice 1's k step 0 in two runs, the restarting run
+//                  [max(zlo, 2+SH), 5] with accumulate off, then the other
+//                  slices' runs up to level 5.
 enum { kStageAll = 0, kStageRestartA = 1, kStageRestartC = 2 };
 template <int S, int SH, int L, int KIND>
 __device__ __forceinline__ void stage_program(uint32_t tmem, uint64_t ad0, uint64_t bd0, int zlo) {
@@ -524,17 +527,28 @@ __device__ __forceinline__ void stage_program(uint32_t tmem, uint64_t ad0, uint6
     slices_full<S, SH, L>(tmem, ad0, bd0, 0, 1, S);
     slices_full<S, SH, L>(tmem, ad0, bd0, 1, 1, S);
   } else if constexpr (KIND == kStageRestartA) {
-    slices_full<S, SH, L>(tmem, ad0, bd0, 0, 5 - SH, S);
-    slices_full<S, SH, L>(tmem, ad0, bd0, 1, 5 - SH, S);
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+      for (int p = 1; p <= S; ++p) {
+        const int top = p + SH + (L - p - SH < S ? L - p - SH : S);
+        const int lo = p + 1 + SH > 6 ? p + 1 + SH : 6;
+        slice_run<S, SH>(tmem, ad0, bd0, p, ks, lo, top, 1u);
+      }
   } else {
     if constexpr (SH <= 3) {   // slice 1 starts at level 2 + SH <= 5
-      const int lo = 2 + SH, hi = (L < 1 + SH + S) ? L : 1 + SH + S;
+      const int lo = 2 + SH, top1 = (L < 1 + SH + S) ? L : 1 + SH + S;
+      const int hi = top1 < 5 ? top1 : 5;
       const int f0 = zlo > lo ? zlo : lo;
-      slice1_run<S, SH>(tmem, ad0, bd0, lo, f0 - 1, 1u);
-      slice1_run<S, SH>(tmem, ad0, bd0, f0, hi < 5 ? hi : 5, 0u);
-      slice1_run<S, SH>(tmem, ad0, bd0, 6, hi, 1u);
-      slices_full<S, SH, L>(tmem, ad0, bd0, 0, 2, 4 - SH);
-      slices_full<S, SH, L>(tmem, ad0, bd0, 1, 1, 4 - SH);
+      slice_run<S, SH>(tmem, ad0, bd0, 1, 0, lo, f0 - 1, 1u);
+      slice_run<S, SH>(tmem, ad0, bd0, 1, 0, f0, hi, 0u);
+#pragma unroll
+      for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+        for (int p = 1 + (1 - ks); p <= 4 - SH; ++p) {
+          const int top = p + SH + (L - p - SH < S ? L - p - SH : S);
+          slice_run<S, SH>(tmem, ad0, bd0, p, ks, p + 1 + SH, top < 5 ? top : 5, 1u);
+        }
     }
   }
 }

@@ -2104,6 +2104,7 @@ namespace tagpu {
 // Device-side work lists of one launch set (kept alive while it may replay).
 struct LaunchBufs {
   DBuf views, items;            // DMMA contraction views and 64x64 work items
+  DBuf derr;                    // DMMA error flag (a bounded stage wait ran out)
   DBuf ozp[8], ozv[8];          // emulated form: parameter blocks, block offsets
   int64_t oz_nblk[8] = {0};
   // emulated form, per digit count: job tables of the grouped zeroing,
@@ -2116,9 +2117,17 @@ struct LaunchBufs {
   bool any_error() const {
     for (OzakiPlan* p : err_owners)
       if (ozaki_error(p)) return true;
+    if (derr.p) {
+      int e = 0;
+      if (cudaMemcpy(&e, derr.p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+      }
+      if (e) return true;
+    }
     return false;
   }
-  explicit LaunchBufs(tagpu_ctx* c) : views(c), items(c) {
+  explicit LaunchBufs(tagpu_ctx* c) : views(c), items(c), derr(c) {
     for (int i = 0; i < 8; ++i) {
       ozp[i].ctx = c;
       ozv[i].ctx = c;
@@ -2151,6 +2160,12 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, Launch
       }
     }
   }
+  // the DMMA loader's bulk copies start up to 8 bytes before a row and rely
+  // on 16-byte aligned operand allocations (device allocations are 256-byte
+  // aligned)
+  for (const GemmView& v : views)
+    if (((uintptr_t)v.A | (uintptr_t)v.B) & 15)
+      return fail(ctx, TAGPU_ERR_INVALID, "plain GEMM: operand storage not 16-byte aligned");
   if (upload) {
     tagpu_status e;
     if ((e = upload_vec(ctx, d_views, views)) || (e = upload_vec(ctx, d_items, items))) return e;
@@ -2223,8 +2238,13 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, Launch
                              S, ozaki_error_flag(g[0]), ctx->sm_count, ctx->wait_ns, stream);
   }
   if (!items.empty()) {
+    if (!lb.derr.p) {
+      tagpu_status e = lb.derr.alloc(sizeof(int));
+      if (e) return e;
+    }
+    CUDA_TRY(ctx, cudaMemsetAsync(lb.derr.p, 0, sizeof(int), stream));
     launch_dmma_gemm(stream, d_views.as<GemmView>(), d_items.as<WorkItem>(),
-                     (int64_t)items.size(), ctx->sm_count);
+                     (int64_t)items.size(), lb.derr.as<int>(), ctx->wait_ns, ctx->sm_count);
     for (auto* c : cs) {
       if (c->emulated()) continue;
       c->st.gemm_blocks = (int64_t)c->items.size();
@@ -2282,6 +2302,8 @@ tagpu_status contract_impl(tagpu_ctx* ctx, const char* c_idx, double alpha, tagp
     tm.stop();
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     c.st.ms_gemm = tm.ms();
+    if (lbuf.any_error())
+      return fail(ctx, TAGPU_ERR_TIMEOUT, "plain GEMM: a bounded stage wait ran out; results invalid");
   }
   fill_stats(c);
   for (OzakiPlan* pl : c.ozs) c.st.mma_flops += ozaki_mma_flops(pl);
