@@ -5,18 +5,16 @@
 // fuses dimensions and runs blocked 2-D transposes (math/transpose.h:178);
 // here every tile is decomposed into work items:
 //   * the argument's fastest dimension stays fastest: items are groups of
-//     consecutive rows of the RESULT, so an item's output is one contiguous
-//     range (the sectors two rows share are written by one CTA at about the
-//     same time), each row copied by a warp from its argument offset;
+//     contiguous rows, copied with coalesced loads and stores;
 //   * otherwise the plane (b, a) of the argument's fastest dimension a and the
 //     dimension b that becomes the result's fastest is cut into 32x32 blocks,
 //     staged through shared memory so that both the load (along a) and the
 //     store (along b) are coalesced; all other dimensions form the batch.
 // All tiles of one array share the permutation; extents differ per tile.
 // Index arithmetic is paid per item, not per element: a row-copy item is
-// kRowsPerItem result rows whose argument offsets are computed once into
-// shared memory; a transpose item is a strip of 32 x 32 blocks along the
-// result's fastest dimension.
+// kRowsPerItem rows whose offsets are computed once into shared memory and
+// then copied as one flat, coalesced element range; a transpose item is a
+// strip of 32 x 32 blocks along the result's fastest dimension.
 #include <cuda_runtime.h>
 
 #include "internal.h"
@@ -86,27 +84,13 @@ __device__ inline void batch_offsets(const TileGeom& g, int rank, int skip0, int
   }
 }
 
-// Argument offset of result row R (all result dims but the fastest, in
-// result order): result dim q is argument dim inv[q].
-__device__ inline int64_t result_row_in_offset(const TileGeom& g, const int* inv, int rank,
-                                               int64_t R) {
-  int64_t in_off = 0;
-  for (int q = rank - 2; q >= 0; --q) {
-    const int x = inv[q];
-    const int64_t ix = R % g.e[x];
-    R /= g.e[x];
-    in_off += ix * g.is[x];
-  }
-  return in_off;
-}
-
 __global__ void __launch_bounds__(256) permute_kernel(
     PermuteDesc d, int64_t ntiles, const int32_t* __restrict__ ext,
     const int64_t* __restrict__ in_off, const int64_t* __restrict__ out_off,
     const int64_t* __restrict__ item_start, int64_t nitems,
     const double* __restrict__ in, double* __restrict__ out) {
   __shared__ double buf[32][33];
-  __shared__ int64_t s_io[kRowsPerItem];
+  __shared__ int64_t s_io[kRowsPerItem], s_oo[kRowsPerItem];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
   for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
     // tile owning this item
@@ -122,22 +106,21 @@ __global__ void __launch_bounds__(256) permute_kernel(
     const double* src = in + in_off[t];
     double* dst = out + out_off[t];
     if (g.a == g.b) {
-      // result rows R0..R0+nr-1: output elements [R0 * rowlen, (R0 + nr) * rowlen)
       const int64_t rowlen = g.e[g.a];
       const int64_t rows = g.vol / rowlen;
-      const int64_t R0 = local * kRowsPerItem;
-      const int nr = (int)(rows - R0 < kRowsPerItem ? rows - R0 : kRowsPerItem);
-      int inv[8];
-      for (int x = 0; x < d.rank; ++x) inv[d.perm[x]] = x;
-      for (int i = threadIdx.x; i < nr; i += blockDim.x)
-        s_io[i] = result_row_in_offset(g, inv, d.rank, R0 + i);
+      const int64_t r0 = local * kRowsPerItem;
+      const int nr = (int)(rows - r0 < kRowsPerItem ? rows - r0 : kRowsPerItem);
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+        int64_t io, oo;
+        batch_offsets(g, d.rank, g.a, -1, r0 + i, io, oo);
+        s_io[i] = io;
+        s_oo[i] = oo;
+      }
       __syncthreads();
-      // one warp per row (16-byte accesses when both ends are aligned); the
-      // item's rows are adjacent in the result, so the sectors two rows
-      // share are written by the same CTA at about the same time
+      // one warp per row; 16-byte accesses when both ends are aligned
       for (int row = ty; row < nr; row += 8) {
         const double* sp = src + s_io[row];
-        double* dp = dst + (R0 + row) * rowlen;
+        double* dp = dst + s_oo[row];
         if (((((uintptr_t)sp) | ((uintptr_t)dp)) & 15) == 0) {
           const int64_t half = rowlen >> 1;
           const double2* s2 = reinterpret_cast<const double2*>(sp);
