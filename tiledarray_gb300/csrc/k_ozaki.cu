@@ -1720,18 +1720,24 @@ __global__ void brick_flag_kernel(OperandView v, const int32_t* __restrict__ row
   flag[x] = f;
 }
 
+// Slot of every flagged (block, k block) x = block * KB + k block, and the
+// list of flagged pairs.  With CBt > 0 the slot map is written transposed,
+// at k block * CBt + block (the B bricks' (k block, column block) order).
 __global__ void brick_slot_kernel(const int64_t* __restrict__ flag,
                                   const int64_t* __restrict__ scan, int64_t n, int64_t KB,
-                                  int32_t* __restrict__ slot, int32_t* __restrict__ list) {
+                                  int32_t* __restrict__ slot, int32_t* __restrict__ list,
+                                  int64_t CBt) {
   const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= n) return;
+  const int64_t blk = x / KB, kb = x - blk * KB;
+  const int64_t at = CBt > 0 ? kb * CBt + blk : x;
   if (flag[x]) {
     const int64_t s = scan[x];
-    slot[x] = (int32_t)s;
-    list[2 * s] = (int32_t)(x / KB);
-    list[2 * s + 1] = (int32_t)(x - (x / KB) * KB);
+    slot[at] = (int32_t)s;
+    list[2 * s] = (int32_t)blk;
+    list[2 * s + 1] = (int32_t)kb;
   } else {
-    slot[x] = -1;
+    slot[at] = -1;
   }
 }
 
@@ -1935,6 +1941,26 @@ struct OzakiPlan {
     tagpu_status st = alloc(p, v.size(), e);
     if (st) return st;
     if (!v.empty()) cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+    return TAGPU_OK;
+  }
+  // Several int32 vectors in one allocation and one copy (each starts on a
+  // 16-byte boundary): fewer host round trips than one upload per vector.
+  tagpu_status upload_many(const std::vector<std::pair<int32_t**, const std::vector<int32_t>*>>& v,
+                           std::string* e) {
+    std::vector<size_t> at;
+    size_t n = 0;
+    for (const auto& x : v) {
+      at.push_back(n);
+      n += (std::max<size_t>(1, x.second->size()) + 3) & ~(size_t)3;
+    }
+    std::vector<int32_t> host(n, 0);
+    for (size_t i = 0; i < v.size(); ++i)
+      std::copy(v[i].second->begin(), v[i].second->end(), host.begin() + at[i]);
+    int32_t* d = nullptr;
+    tagpu_status st = alloc(&d, n, e);
+    if (st) return st;
+    cudaMemcpyAsync(d, host.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, s);
+    for (size_t i = 0; i < v.size(); ++i) *v[i].first = d + at[i];
     return TAGPU_OK;
   }
 };
@@ -2192,14 +2218,13 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
     return e;
   };
   tagpu_status st;
-  if ((st = pl->upload(&pl->row_ext, extents(rt, h_msz), err)) ||
-      (st = pl->upload(&pl->k_ext, extents(kt_, h_ksz), err)) ||
-      (st = pl->upload(&pl->col_ext, extents(ct, h_nsz), err)))
-    return st;
-  if ((st = pl->upload(&pl->row_tile, rt, err)) || (st = pl->upload(&pl->row_local, rl, err)) ||
-      (st = pl->upload(&pl->rstart, rs, err)) || (st = pl->upload(&pl->k_tile, kt_, err)) ||
-      (st = pl->upload(&pl->k_local, kl, err)) || (st = pl->upload(&pl->col_tile, ct, err)) ||
-      (st = pl->upload(&pl->col_local, cl, err)) || (st = pl->upload(&pl->cstart, cs, err)) ||
+  const std::vector<int32_t> row_e = extents(rt, h_msz), k_e = extents(kt_, h_ksz),
+                             col_e = extents(ct, h_nsz);
+  if ((st = pl->upload_many({{&pl->row_ext, &row_e}, {&pl->k_ext, &k_e}, {&pl->col_ext, &col_e},
+                             {&pl->row_tile, &rt}, {&pl->row_local, &rl}, {&pl->rstart, &rs},
+                             {&pl->k_tile, &kt_}, {&pl->k_local, &kl}, {&pl->col_tile, &ct},
+                             {&pl->col_local, &cl}, {&pl->cstart, &cs}},
+                            err)) ||
       (st = pl->alloc(&pl->EA, pl->M_total, err)) || (st = pl->alloc(&pl->EB, pl->N_total, err)) ||
       (st = pl->alloc(&pl->err, 1, err)))
     return st;
@@ -2226,12 +2251,11 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   b.ksz = v.ksz;
   b.row_contig = v.b_trans ? 0 : 1;  // k x n storage: rows (n) contiguous
   b.hel = v.hel;
-  // brick maps
-  int64_t* flag = nullptr;
-  int64_t* scan = nullptr;
+  // brick maps: A and B flag passes, one host read of both counts
+  int64_t *flag = nullptr, *scan = nullptr, *flag_b = nullptr, *scan_b0 = nullptr;
   const int64_t nfa = pl->RB * pl->KB, nfb = pl->CB * pl->KB;
-  const int64_t nf = std::max(nfa, nfb);
-  if ((st = pl->alloc(&flag, nf, err)) || (st = pl->alloc(&scan, nf + 1, err)) ||
+  if ((st = pl->alloc(&flag, nfa, err)) || (st = pl->alloc(&scan, nfa + 1, err)) ||
+      (st = pl->alloc(&flag_b, nfb, err)) || (st = pl->alloc(&scan_b0, nfb + 1, err)) ||
       (st = pl->alloc(&pl->brickA, nfa, err)) || (st = pl->alloc(&pl->listA, 2 * nfa, err)) ||
       (st = pl->alloc(&pl->brickB, nfb, err)) || (st = pl->alloc(&pl->listB, 2 * nfb, err)))
     return st;
@@ -2240,43 +2264,32 @@ tagpu_status ozaki_plan(cudaStream_t s, const GemmView& v, const int32_t* h_msz,
   count_launch();
   launch_exclusive_scan(s, flag, nfa, scan);
   brick_slot_kernel<<<blocks_for(nfa, 256), 256, 0, s>>>(flag, scan, nfa, pl->KB, pl->brickA,
-                                                         pl->listA);
+                                                         pl->listA, 0);
+  count_launch();
+  // B bricks are indexed (k block, column block) in the GEMM; the flag pass
+  // runs over (column block, k block) and the slots are written transposed
+  brick_flag_kernel<<<blocks_for(nfb, 256), 256, 0, s>>>(b, pl->col_tile, pl->k_tile,
+                                                         pl->N_total, pl->K_total, BN, pl->CB,
+                                                         pl->KB, flag_b);
+  count_launch();
+  launch_exclusive_scan(s, flag_b, nfb, scan_b0);
+  brick_slot_kernel<<<blocks_for(nfb, 256), 256, 0, s>>>(flag_b, scan_b0, nfb, pl->KB,
+                                                         pl->brickB, pl->listB, pl->CB);
   count_launch();
   cudaMemcpyAsync(&pl->nA, scan + nfa, 8, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(&pl->nB, scan_b0 + nfb, 8, cudaMemcpyDeviceToHost, s);
   cudaStreamSynchronize(s);
-  // B bricks are indexed (k block, column block) in the GEMM; the flag pass
-  // runs over (column block, k block) and is transposed into brickB
-  {
-    int32_t* slot_cb = nullptr;
-    if ((st = pl->alloc(&slot_cb, nfb, err))) return st;
-    brick_flag_kernel<<<blocks_for(nfb, 256), 256, 0, s>>>(b, pl->col_tile, pl->k_tile,
-                                                           pl->N_total, pl->K_total, BN, pl->CB,
-                                                           pl->KB, flag);
+  if ((st = pl->alloc(&pl->hdrA, pl->nA, err)) || (st = pl->alloc(&pl->hdrB, pl->nB, err)))
+    return st;
+  if (pl->nA) {
+    brick_hdr_kernel<<<blocks_for(pl->nA, 256), 256, 0, s>>>(
+        pl->listA, pl->nA, pl->row_tile, pl->k_tile, pl->M_total, pl->K_total, BM, pl->hdrA);
     count_launch();
-    launch_exclusive_scan(s, flag, nfb, scan);
-    brick_slot_kernel<<<blocks_for(nfb, 256), 256, 0, s>>>(flag, scan, nfb, pl->KB, slot_cb,
-                                                           pl->listB);
+  }
+  if (pl->nB) {
+    brick_hdr_kernel<<<blocks_for(pl->nB, 256), 256, 0, s>>>(
+        pl->listB, pl->nB, pl->col_tile, pl->k_tile, pl->N_total, pl->K_total, BN, pl->hdrB);
     count_launch();
-    cudaMemcpyAsync(&pl->nB, scan + nfb, 8, cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-    if ((st = pl->alloc(&pl->hdrA, pl->nA, err)) || (st = pl->alloc(&pl->hdrB, pl->nB, err)))
-      return st;
-    if (pl->nA) {
-      brick_hdr_kernel<<<blocks_for(pl->nA, 256), 256, 0, s>>>(
-          pl->listA, pl->nA, pl->row_tile, pl->k_tile, pl->M_total, pl->K_total, BM, pl->hdrA);
-      count_launch();
-    }
-    if (pl->nB) {
-      brick_hdr_kernel<<<blocks_for(pl->nB, 256), 256, 0, s>>>(
-          pl->listB, pl->nB, pl->col_tile, pl->k_tile, pl->N_total, pl->K_total, BN, pl->hdrB);
-      count_launch();
-    }
-    std::vector<int32_t> h(nfb), t(nfb);
-    cudaMemcpyAsync(h.data(), slot_cb, nfb * 4, cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-    for (int64_t cb = 0; cb < pl->CB; ++cb)
-      for (int64_t kb = 0; kb < pl->KB; ++kb) t[kb * pl->CB + cb] = h[cb * pl->KB + kb];
-    cudaMemcpyAsync(pl->brickB, t.data(), nfb * 4, cudaMemcpyHostToDevice, s);
   }
   // units (pairs of output blocks) and their k-block lists
   const int64_t CP = (pl->CB + 1) / 2;
