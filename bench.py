@@ -526,7 +526,8 @@ def run_serve(args, w, ta, wl, prec):
     shape but no storage and must come back rejected.  Requests pick a family
     (weights --mix) and then a pool entry of it uniformly.  A sample of the
     served results (those under 0.5 TFLOP) is checked against the plain FP64
-    form after the stream."""
+    form after the stream.  --rate a,b,c sweeps the arrival rate: one stream
+    of --requests requests per rate, each through a fresh server."""
     import threading
     rng = np.random.default_rng(args.seed)
     thr = 1e-8
@@ -563,87 +564,106 @@ def run_serve(args, w, ta, wl, prec):
     fams = ["blocksparse", "ccsd", "batched"]
     mix = np.asarray([float(x) for x in args.mix.split(",")])
     mix = mix / mix.sum()
-    srv = ta.Server(w, hbm_budget_bytes=budget, max_batch=32, precision=prec,
-                    slices=args.slices)
-    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, args.requests))
-    fam_pick = rng.choice(3, size=args.requests, p=mix)
-    picks = [pool[fams[f]][int(rng.integers(0, len(pool[fams[f]])))] for f in fam_pick]
-    ids, rejected = [None] * args.requests, {}
-    t0 = time.perf_counter()
-    submitted = [0]
+    rates = [float(x) for x in str(args.rate).split(",")]
 
-    def submitter():
-        for x in range(args.requests):
-            dt = arrivals[x] - (time.perf_counter() - t0)
-            if dt > 0:
-                time.sleep(dt)
-            c, A, a, B, b, name = picks[x]
-            try:
-                ids[x] = srv.submit(c, 1.0, A, a, B, b)
-            except ta.TAGPUError as e:
-                key = f"{name}: status {e.status}"
-                rejected[key] = rejected.get(key, 0) + 1
-            submitted[0] = x + 1
+    def stream(rate, seed):
+        """One Poisson stream of args.requests requests at `rate` per second
+        through a fresh server; returns its measurements."""
+        srng = np.random.default_rng(seed)
+        srv = ta.Server(w, hbm_budget_bytes=budget, max_batch=32, precision=prec,
+                        slices=args.slices)
+        arrivals = np.cumsum(srng.exponential(1.0 / rate, args.requests))
+        fam_pick = srng.choice(3, size=args.requests, p=mix)
+        picks = [pool[fams[f]][int(srng.integers(0, len(pool[fams[f]])))] for f in fam_pick]
+        ids, rejected = [None] * args.requests, {}
+        t0 = time.perf_counter()
+        submitted = [0]
 
-    # the clients take their results as they complete (in submission order),
-    # so finished results do not pile up in HBM; a sample is kept for the
-    # check against the plain form
-    results, failures, kept = [], {}, []
+        def submitter():
+            for x in range(args.requests):
+                dt = arrivals[x] - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                c, A, a, B, b, name = picks[x]
+                try:
+                    ids[x] = srv.submit(c, 1.0, A, a, B, b)
+                except ta.TAGPUError as e:
+                    key = f"{name}: status {e.status}"
+                    rejected[key] = rejected.get(key, 0) + 1
+                submitted[0] = x + 1
 
-    def collector():
-        for x in range(args.requests):
-            while submitted[0] <= x:
-                time.sleep(0.0005)
-            if ids[x] is None:
-                continue
-            try:
-                C, res = srv.wait(ids[x], 600000)
-            except ta.TAGPUError as e:
-                # the request failed on the device side (its status and the
-                # server's message); the stream goes on
-                key = f"{picks[x][5]}: status {e.status}"
-                failures[key] = failures.get(key, 0) + 1
-                continue
-            results.append(res)
-            if res["status"] != 0:
-                key = f"{picks[x][5]}: status {res['status']}"
-                failures[key] = failures.get(key, 0) + 1
-            elif len(kept) < args.check and res["flops"] < 5e11 and x % 7 == 0:
-                kept.append((x, C))
-                continue
-            del C
-    th = threading.Thread(target=submitter)
-    tc = threading.Thread(target=collector)
-    th.start()
-    tc.start()
-    th.join()
-    tc.join()
-    wall = time.perf_counter() - t0
-    st = srv.stats()
-    srv.stop()
-    # each kept result against the plain FP64 form of the same contraction
-    worst = 0.0
-    for x, C in kept:
-        c, A, a, B, b, _ = picks[x]
-        Cp, _ = ta.contract(w, c, 1.0, A, a, B, b, precision=ta.PRECISION_FP64)
-        y, z = C.download(), Cp.download()
-        worst = max(worst, float(np.linalg.norm(y - z) / max(np.linalg.norm(z), 1e-300)))
-        del Cp, C
-    flops = sum(r["flops"] for r in results)
-    nrej = sum(rejected.values())
-    _line(args, "served nonzero-block TFLOP/s; p50/p99 latency", flops / wall / 1e12, "TFLOP/s",
-          wall * 1e3 / max(1, len(results)),
-          {"workload": f"{args.requests} Poisson requests at {args.rate}/s, families "
-                       f"block-sparse/ccsd-like/batched in proportion {args.mix}, scales "
-                       "U[0.25,1] (ccsd-like at six scales over [0.25,1]), 150 GB admission "
-                       "budget, one persistent served GEMM", "precision": args.precision,
-                       "slices": args.slices},
-          {"latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"], "mean": st["mean_ms"]},
-           "requests_per_s": len(results) / wall, "completed": st["completed"],
-           "rejected": nrej, "rejected_by_kind": rejected, "failed": st["failed"],
-           "failures": failures, "kernel_waves": st["batches"],
-           "peak_admitted_bytes": st["peak_bytes"],
-           "checked_vs_plain": {"requests": len(kept), "max_rel_err": worst}})
+        # the clients take their results as they complete (in submission
+        # order), so finished results do not pile up in HBM; a sample is kept
+        # for the check against the plain form
+        results, failures, kept = [], {}, []
+
+        def collector():
+            for x in range(args.requests):
+                while submitted[0] <= x:
+                    time.sleep(0.0005)
+                if ids[x] is None:
+                    continue
+                try:
+                    C, res = srv.wait(ids[x], 600000)
+                except ta.TAGPUError as e:
+                    # the request failed on the device side (its status and the
+                    # server's message); the stream goes on
+                    key = f"{picks[x][5]}: status {e.status}"
+                    failures[key] = failures.get(key, 0) + 1
+                    continue
+                results.append(res)
+                if res["status"] != 0:
+                    key = f"{picks[x][5]}: status {res['status']}"
+                    failures[key] = failures.get(key, 0) + 1
+                elif len(kept) < args.check and res["flops"] < 5e11 and x % 7 == 0:
+                    kept.append((x, C))
+                    continue
+                del C
+        th = threading.Thread(target=submitter)
+        tc = threading.Thread(target=collector)
+        th.start()
+        tc.start()
+        th.join()
+        tc.join()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.stop()
+        # each kept result against the plain FP64 form of the same contraction
+        worst = 0.0
+        for x, C in kept:
+            c, A, a, B, b, _ = picks[x]
+            Cp, _ = ta.contract(w, c, 1.0, A, a, B, b, precision=ta.PRECISION_FP64)
+            y, z = C.download(), Cp.download()
+            worst = max(worst, float(np.linalg.norm(y - z) / max(np.linalg.norm(z), 1e-300)))
+            del Cp, C
+        flops = sum(r["flops"] for r in results)
+        return {"rate": rate, "tflops": flops / wall / 1e12, "wall_s": wall,
+                "requests_per_s": len(results) / wall,
+                "latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"], "mean": st["mean_ms"]},
+                "completed": st["completed"], "rejected": sum(rejected.values()),
+                "rejected_by_kind": rejected, "failed": st["failed"], "failures": failures,
+                "kernel_waves": st["batches"], "peak_admitted_bytes": st["peak_bytes"],
+                "checked_vs_plain": {"requests": len(kept), "max_rel_err": worst},
+                "ms_per_request": wall * 1e3 / max(1, len(results))}
+
+    sweep = [stream(r, args.seed + 17 * k) for k, r in enumerate(rates)]
+    top = sweep[-1]
+    extra = {k: top[k] for k in ("latency_ms", "requests_per_s", "completed", "rejected",
+                                 "rejected_by_kind", "failed", "failures", "kernel_waves",
+                                 "peak_admitted_bytes", "checked_vs_plain")}
+    if len(sweep) > 1:
+        extra["sweep"] = [{k: r[k] for k in ("rate", "tflops", "requests_per_s", "latency_ms",
+                                             "completed", "rejected", "failed",
+                                             "checked_vs_plain")} for r in sweep]
+    _line(args, "served nonzero-block TFLOP/s; p50/p99 latency", top["tflops"], "TFLOP/s",
+          top["ms_per_request"],
+          {"workload": f"{args.requests} Poisson requests at {top['rate']}/s"
+                       + (f" (also at {', '.join(str(r) for r in rates[:-1])}/s, same count)"
+                          if len(rates) > 1 else "")
+                       + f", families block-sparse/ccsd-like/batched in proportion {args.mix}, "
+                       "scales U[0.25,1] (ccsd-like at six scales over [0.25,1]), 150 GB "
+                       "admission budget, one persistent served GEMM",
+           "precision": args.precision, "slices": args.slices}, extra)
 
 
 def main():
@@ -671,7 +691,8 @@ def main():
                     help="ccsd: operand index order (general = explicit tile permutation)")
     ap.add_argument("--count", type=int, default=512, help="batched: contractions")
     ap.add_argument("--requests", type=int, default=300, help="serve: requests")
-    ap.add_argument("--rate", type=float, default=40.0, help="serve: Poisson arrivals / s")
+    ap.add_argument("--rate", default="20", help="serve: Poisson arrivals / s; a comma list "
+                    "sweeps the rates, one stream each (the last is the line's headline)")
     ap.add_argument("--mix", default="4,1,5",
                     help="serve: weights of the block-sparse, ccsd-like and batched families")
     ap.add_argument("--check", type=int, default=24,
