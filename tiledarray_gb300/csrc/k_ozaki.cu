@@ -237,54 +237,43 @@ __host__ __device__ constexpr uint32_t idesc_n(int n) {
          ((uint32_t)(BM >> 4) << 24);
 }
 
-// Correctly rounded double of (hi * 2^sh + lo) * 2^e2 from exact integers
-// (|hi| < 2^61, |lo| < 2^62, 0 <= sh < 64), with integer instructions only;
-// FP64 arithmetic on this GPU is far slower than integer arithmetic.  The
-// rare results outside the normal range take the FP64 library route.
-__device__ __forceinline__ double exact_to_double(int64_t hi, int64_t lo, int sh, int e2) {
-  // W = hi * 2^sh + lo as a 128-bit two's complement wh:wl
-  const uint64_t hl = (uint64_t)hi << sh;
-  int64_t wh = sh ? (hi >> (64 - sh)) : (hi >> 63);
-  const uint64_t wl = hl + (uint64_t)lo;
-  wh += (lo >> 63) + (int64_t)(wl < hl);
-  const bool neg = wh < 0;
-  uint64_t mh = (uint64_t)wh, ml = wl;   // |W|
-  if (neg) {
-    ml = ~ml + 1;
-    mh = ~mh + (ml == 0 ? 1 : 0);
-  }
-  // top: the 64 bits from the leading one down; sticky: any one below them;
-  // p: position of the leading one in W
-  uint64_t top;
-  bool sticky;
-  int p;
-  if (mh) {
-    const int lz = __clzll((long long)mh);
-    top = lz ? (mh << lz) | (ml >> (64 - lz)) : mh;
-    sticky = (lz ? (ml << lz) : ml) != 0;
-    p = 127 - lz;
+// Correctly rounded double of (hi * 2^SH + lo) * 2^e2 from exact integers
+// (|hi| < 2^61, |lo| < 2^62, 0 <= SH <= 32).  The value is first cut to a
+// signed 64-bit window with the bits cut off ORed into its lowest bit
+// (rounding to odd, which a later rounding to 53 bits turns into the correct
+// rounding of the exact value, as the window keeps at least 55 bits); one
+// conversion instruction then rounds the window to nearest even and an
+// integer add on the exponent field scales it.  Rounding to odd needs no
+// separate magnitude: in two's complement, truncating toward minus infinity
+// and setting the lowest bit when anything was cut picks the odd neighbour
+// for either sign.  The rare results outside the normal range take the FP64
+// library route.
+template <int SH>
+__device__ __forceinline__ double exact_to_double(int64_t hi, int64_t lo, int e2) {
+  static_assert(SH >= 0 && SH <= 32, "shift between the accumulators");
+  int64_t y;
+  int scale = e2;
+  if constexpr (SH == 0) {
+    y = hi + lo;
   } else {
-    if (!ml) return 0.0;
-    const int lz = __clzll((long long)ml);
-    top = ml << lz;
-    sticky = false;
-    p = 63 - lz;
+    // W = H * 2^SH + r with 0 <= r < 2^SH
+    const int64_t H = hi + (lo >> SH);
+    const uint32_t r = SH == 32 ? (uint32_t)lo : ((uint32_t)lo & ((1u << (SH & 31)) - 1u));
+    const int s = __clzll((long long)(H ^ (H >> 63))) - 1;   // redundant sign bits of H
+    if (s >= SH) {   // W fits in 64 bits
+      y = (int64_t)(((uint64_t)H << SH) | r);
+    } else {
+      const int d = SH - s;   // bits of r below the window, 1..SH
+      y = (int64_t)(((uint64_t)H << s) | ((uint64_t)r >> d) | ((uint32_t)(r << (32 - d)) != 0u ? 1u : 0u));
+      scale += d;
+    }
   }
-  // round to 53 bits, nearest even
-  uint64_t mant = top >> 11;
-  const uint64_t rem = top & 0x7FF;
-  mant += (rem > 0x400 || (rem == 0x400 && (sticky || (mant & 1)))) ? 1 : 0;
-  int ex = p + e2;   // value = mant * 2^(ex - 52)
-  if (mant >> 53) {  // rounding carried into a new bit
-    mant >>= 1;
-    ++ex;
-  }
-  if (ex < -1022 || ex > 1023) {
-    const double v = ldexp((double)(int64_t)mant, ex - 52);
-    return neg ? -v : v;
-  }
-  const uint64_t bits = ((uint64_t)(ex + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull);
-  return __longlong_as_double((long long)(bits | (neg ? (1ull << 63) : 0)));
+  if (y == 0) return 0.0;
+  const double w = __ll2double_rn((long long)y);
+  const long long bits = __double_as_longlong(w);
+  const int ex = (int)((bits >> 52) & 0x7ff) + scale;
+  if (ex < 1 || ex > 2046) return ldexp(w, scale);
+  return __longlong_as_double(bits + ((long long)scale << 52));
 }
 
 
@@ -1148,7 +1137,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
           for (int c = 0; c < 16; ++c) {
             const int j = 16 * hc + c;
             const int eb = __shfl_sync(full, eb_l, j);
-            const double v = exact_to_double(hi[j], lo[j], 8 * (TOP - kExactTop), e2 + eb);
+            const double v = exact_to_double<8 * (TOP - kExactTop)>(hi[j], lo[j], e2 + eb);
             sb[lane * EPI_LD + c] = alpha == 1.0 ? v : alpha * v;
           }
           __syncwarp();
