@@ -336,6 +336,16 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def tensor_roofline(mma, ms, kernel):
+    """Roofline object of the emulated form's tensor work: the bf16 flops of
+    the digit-slice MMAs issued (`mma_flops`) over a CUDA-event time `ms`."""
+    _, bf16_peak, peak_kind = peaks()
+    achieved = mma / (ms * 1e-3) / 1e12
+    return {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+            "frac": achieved / bf16_peak, "traffic": None, "kernel": kernel,
+            "peak_kind": f"{peak_kind} bf16 burst", "mma_flops_per_step": mma}
+
+
 def _line(args, metric, value, unit, ms, cfg, extra):
     out = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -414,10 +424,14 @@ def run_secondary(args):
         C, st = res["c"]
         err, stp = err_vs_plain(C, "i,j", A, "i,k", B, "k,j")
         m = statistics.median(ms)
+        extra = {"rel_err_vs_plain_fp64": err, "plain_ms": stp["ms_total"],
+                 "phases_ms": {k: st[k] for k in ("ms_shape", "ms_pairs", "ms_split", "ms_gemm")}}
+        if prec == ta.PRECISION_OZAKI and st["mma_flops"]:
+            extra["roofline"] = tensor_roofline(st["mma_flops"], st["ms_gemm"],
+                                                "ozaki_gemm (bf16 digit-slice MMAs issued)")
         _line(args, "dense TFLOP/s", st["flops"] / m / 1e9, "TFLOP/s", m,
               {"workload": "dense TArrayD 2048^3, tiles 128", "precision": args.precision},
-              {"rel_err_vs_plain_fp64": err, "plain_ms": stp["ms_total"],
-               "phases_ms": {k: st[k] for k in ("ms_shape", "ms_pairs", "ms_split", "ms_gemm")}})
+              extra)
     elif args.workload == "ccsd":
         hv, ho, vs, ts = wl.ccsd(v=args.v, seed=args.seed)
         thr = 1e-8
@@ -444,6 +458,9 @@ def run_secondary(args):
                                                   "ms_split", "ms_gemm")},
                  "pairs": st["pairs"], "flops_per_step": st["flops"],
                  "permtypes": [st["left_permtype"], st["right_permtype"]]}
+        if prec == ta.PRECISION_OZAKI and st["mma_flops"]:
+            extra["roofline"] = tensor_roofline(st["mma_flops"], st["ms_gemm"],
+                                                "ozaki_gemm (bf16 digit-slice MMAs issued)")
         if st["left_permtype"] == 3 and st["ms_permute"] > 0:
             moved = 16.0 * V.info().elements
             extra["permute"] = {"bytes": moved, "GB_per_s": moved / st["ms_permute"] / 1e6,
@@ -495,6 +512,12 @@ def run_secondary(args):
         extra = {"flops_per_step": bst.flops, "pairs": bst.pairs, "plan_and_capture_s": plan_s,
                  "latency_ms": {"p50": float(np.percentile(ms, 50)),
                                 "p99": float(np.percentile(ms, 99))}}
+        if prec == ta.PRECISION_OZAKI and bst.mma_flops:
+            # the GEMM launches run inside the captured graph: the time is
+            # the whole replay (frames, splits and GEMMs)
+            extra["roofline"] = tensor_roofline(
+                bst.mma_flops, m, "graph replay: ozaki_gemm MMAs issued over the whole replay "
+                                  "(frame, split and GEMM launches)")
         if not args.no_plain and prec == ta.PRECISION_OZAKI:
             pms, _, _, pouts = batch(ta.PRECISION_FP64, 1, 1)
             x = np.concatenate([o.download() for o in outs])

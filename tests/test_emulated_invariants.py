@@ -1,10 +1,11 @@
 """Host-side checks of the integer invariants the emulated-FP64 kernels rely
-on, restated in Python: the balanced base-256 digit split (64-bit recurrence
-and the 32-bit two-part form the split kernel uses give the same digits,
-and the digits rebuild the fixed-point value), and the level restart
+on, restated in Python: the balanced base-256 digit split (the 64-bit
+recurrence and the biased-byte form the split kernel uses give the same
+digits, and the digits rebuild the fixed-point value), and the level restart
 periods (every exact level stays within 2^24, restarting levels form one
 run of adjacent levels)."""
 import random
+import struct
 
 import pytest
 
@@ -20,46 +21,28 @@ def digits_64(fx, S):
     return h
 
 
-def to_i32(x):
-    x &= 0xFFFFFFFF
-    return x - (1 << 32) if x >= 1 << 31 else x
+def f32(x):
+    """float32 rounding of a Python float (round to nearest even)."""
+    return struct.unpack("<f", struct.pack("<f", x))[0]
 
 
-def digits_32(fx, S):
-    """The split kernel's form: all in 32 bits for S <= 3; otherwise the low
-    three digits from the low 24 bits, their carry into the high part."""
+def digits_bias(fx, S):
+    """The split kernel's form: 128 added at each of the S - 1 lower digit
+    positions of the 64-bit two's complement value; lower digit q is byte q
+    of the sum minus 128, computed as the float (2^23 + byte) - (2^23 + 128)
+    (a byte permute into 0x4B0000xx and one float add); the top digit is the
+    sum shifted down arithmetically by 8 (S - 1)."""
+    bias = 0x8080808080808080 >> (8 * (9 - S))
+    u = (fx + bias) & 0xFFFFFFFFFFFFFFFF
     h = [0] * S
-
-    def step(v):
-        d = ((v + 128) & 255) - 128
-        return d, (v - d) >> 8
-    if S <= 3:
-        v = to_i32(fx)
-        for p in range(S - 1, 0, -1):
-            h[p], v = step(v)
-        h[0] = v
-        return h
-    if S <= 6:
-        lo, hi = to_i32(fx & 0xFFFFFF), to_i32(fx >> 24)
-        for p in range(S - 1, S - 4, -1):
-            h[p], lo = step(lo)
-        hi += lo
-        for p in range(S - 4, 0, -1):
-            h[p], hi = step(hi)
-        h[0] = hi
-        return h
-    # S = 7 (|fx| <= 2^55): three 32-bit parts, the low two of 24 bits, each
-    # part's carry joining the next
-    lo, mid, top = to_i32(fx & 0xFFFFFF), to_i32((fx >> 24) & 0xFFFFFF), to_i32(fx >> 48)
-    for p in range(S - 1, S - 4, -1):
-        h[p], lo = step(lo)
-    mid += lo
-    for p in range(S - 4, S - 7, -1):
-        h[p], mid = step(mid)
-    top += mid
-    for p in range(S - 7, 0, -1):
-        h[p], top = step(top)
-    h[0] = top
+    for q in range(S - 1):
+        byte = (u >> (8 * q)) & 255
+        as_float = struct.unpack("<f", struct.pack("<I", 0x4B000000 | byte))[0]
+        d = f32(as_float - 8388736.0)
+        assert d == int(d)
+        h[S - 1 - q] = int(d)
+    top = u - (1 << 64) if u >= 1 << 63 else u
+    h[0] = top >> (8 * (S - 1))
     return h
 
 
@@ -72,8 +55,8 @@ def test_digit_split_forms_agree(S):
              (1 << 48) - 1, 1 << 48, -(1 << 48), (1 << 48) + (1 << 24) - 128, -(1 << 48) - 129]
     values = [v for v in edges if abs(v) <= lim] + [rng.randint(-lim, lim) for _ in range(20000)]
     for fx in values:
-        d64, d32 = digits_64(fx, S), digits_32(fx, S)
-        assert d64 == d32, fx
+        d64, dk = digits_64(fx, S), digits_bias(fx, S)
+        assert d64 == dk, fx
         assert all(abs(d) <= 128 for d in d64), fx          # exact in bf16, |d e| <= 2^14
         assert sum(d * 256 ** (S - 1 - p) for p, d in enumerate(d64)) == fx
 

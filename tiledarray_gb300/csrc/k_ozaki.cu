@@ -1125,6 +1125,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
         const int64_t Nt = P.Nt;
         double* __restrict__ const Cout = P.C;
         const double alpha = P.alpha;
+        const bool unit_alpha = alpha == 1.0;
         double* sb = reinterpret_cast<double*>(stage_base + STAGES * STAGE_BYTES) +
                      (warp - 2) * 32 * EPI_LD;
         // Two passes of 16 columns: each lane converts its row's values into
@@ -1138,7 +1139,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
             const int j = 16 * hc + c;
             const int eb = __shfl_sync(full, eb_l, j);
             const double v = exact_to_double<8 * (TOP - kExactTop)>(hi[j], lo[j], e2 + eb);
-            sb[lane * EPI_LD + c] = alpha == 1.0 ? v : alpha * v;
+            sb[lane * EPI_LD + c] = unit_alpha ? v : alpha * v;
           }
           __syncwarp();
           const int c = lane & 15;
@@ -1369,10 +1370,11 @@ __global__ void zero_kernel(const ZeroJob* __restrict__ jobs) {
 }
 
 // Digits of one element: fixed point round(x * 2^(8S-1-E)) (E = frame -
-// 1022), cut into S balanced base-256 digits, least significant first, each
-// returned as the bit pattern of the exact bf16 (|d| <= 128).
+// 1022), cut into S balanced base-256 digits, f[0] the most significant,
+// each returned as the bit pattern of the exact float (|d| <= 128), whose
+// high half is the bf16 digit and whose low half is zero.
 template <int S>
-__device__ __forceinline__ void split_digits(double x, int frame, uint32_t (&h)[S]) {
+__device__ __forceinline__ void split_digits(double x, int frame, uint32_t (&f)[S]) {
   int64_t fx = 0;
   const uint64_t bits = (uint64_t)__double_as_longlong(x);
   const int be = (int)((bits >> 52) & 0x7ff);
@@ -1396,47 +1398,22 @@ __device__ __forceinline__ void split_digits(double x, int frame, uint32_t (&h)[
     }
     fx = (bits >> 63) ? -(int64_t)q : (int64_t)q;
   }
-  // d = ((v + 128) & 255) - 128, v = (v - d) / 256 from the least
-  // significant digit.  |fx| <= 2^(8S-1): for S <= 3 all in 32 bits; else the
-  // low three digits come from the low 24 bits and their carry (0 or 1)
-  // joins the high part, which gives the same digits as the recurrence on
-  // the whole 64-bit value (each step only reads the low 8 bits, and the
-  // high part contributes none of them until it is reached).
-  auto digit = [](int& v) {
-    const int d = ((v + 128) & 255) - 128;
-    v = (v - d) >> 8;
-    return __float_as_uint((float)d) >> 16;
-  };
-  if constexpr (S <= 3) {
-    int v = (int)fx;
+  // The balanced digits of the recurrence d = ((v + 128) & 255) - 128,
+  // v = (v - d) / 256 from the least significant digit: adding 128 at each of
+  // the S - 1 lower digit positions makes digit q (counted from the least
+  // significant) byte q of the sum minus 128, and leaves the top digit as the
+  // sum shifted down by 8 (S - 1).  |fx| <= 2^(8S-1), so the sum does not
+  // overflow.  A byte b becomes the float b - 128 exactly as
+  // (2^23 + b) - (2^23 + 128): one byte permute and one float add.
+  constexpr uint64_t kBias = 0x8080808080808080ull >> (8 * (9 - S));
+  const uint64_t u = (uint64_t)fx + kBias;
+  const uint32_t ul = (uint32_t)u, uh = (uint32_t)(u >> 32);
 #pragma unroll
-    for (int p = S - 1; p >= 1; --p) h[p] = digit(v);
-    h[0] = __float_as_uint((float)v) >> 16;
-  } else if constexpr (S <= 6) {
-    int lo = (int)(fx & 0xFFFFFF);
-    int hi = (int)(fx >> 24);
-#pragma unroll
-    for (int p = S - 1; p >= S - 3; --p) h[p] = digit(lo);
-    hi += lo;
-#pragma unroll
-    for (int p = S - 4; p >= 1; --p) h[p] = digit(hi);
-    h[0] = __float_as_uint((float)hi) >> 16;
-  } else {
-    // |fx| <= 2^55: three digits from each of the two low 24-bit parts, each
-    // part's carry (0 or 1) joining the next, the rest from the top part
-    int lo = (int)(fx & 0xFFFFFF);
-    int mid = (int)((fx >> 24) & 0xFFFFFF);
-    int top = (int)(fx >> 48);
-#pragma unroll
-    for (int p = S - 1; p >= S - 3; --p) h[p] = digit(lo);
-    mid += lo;
-#pragma unroll
-    for (int p = S - 4; p >= S - 6; --p) h[p] = digit(mid);
-    top += mid;
-#pragma unroll
-    for (int p = S - 7; p >= 1; --p) h[p] = digit(top);
-    h[0] = __float_as_uint((float)top) >> 16;
-  }
+  for (int q = 0; q < S - 1; ++q)
+    f[S - 1 - q] = __float_as_uint(
+        __fadd_rn(__uint_as_float(__byte_perm(q < 4 ? ul : uh, 0x4B000000u, 0x7540u | (q & 3))),
+                  -8388736.0f));
+  f[0] = __float_as_uint((float)(int)((int64_t)u >> (8 * (S - 1))));
 }
 
 // A split job: the bricks of one operand (or of one row chunk of it) of one
@@ -1618,8 +1595,12 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 4 : 5) split_kernel(const Sp
     // are cut against 2^(frame - 8m), m = floor(e / 8) whole digits.
     {
       int eloc = kNoShift;
+      // nonzero tested on the bit pattern (±0 is zero): an FP64 compare
+      // would run on this GPU's narrow FP64 pipe once per element
       auto see = [&](double val, int fr) {
-        if (val != 0.0 && fr > 0) eloc = min(eloc, fr - max(exp_field(val), 1));
+        const uint64_t bits = (uint64_t)__double_as_longlong(val);
+        if ((bits << 1) != 0 && fr > 0)
+          eloc = min(eloc, fr - max((int)((bits >> 52) & 0x7ff), 1));
       };
       if (!v.row_contig) {
 #pragma unroll
@@ -1648,7 +1629,7 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 4 : 5) split_kernel(const Sp
         split_digits<S>(x[i], s_fr[r] - dfr, h);
 #pragma unroll
         for (int p = 0; p < S; ++p)
-          *reinterpret_cast<uint16_t*>(c0 + r * 16 + p * SPAD) = (uint16_t)h[p];
+          *reinterpret_cast<uint16_t*>(c0 + r * 16 + p * SPAD) = (uint16_t)(h[p] >> 16);
       }
     } else {
 #pragma unroll
@@ -1657,13 +1638,13 @@ __global__ void __launch_bounds__(256, ROWS == BM ? 4 : 5) split_kernel(const Sp
         const int fr = s_fr[r] - dfr;
         uint32_t w[S][4];
 #pragma unroll
-        for (int p = 0; p < S; ++p) w[p][0] = w[p][1] = w[p][2] = w[p][3] = 0;
+        for (int j = 0; j < 8; j += 2) {
+          uint32_t h0[S], h1[S];
+          split_digits<S>(x[8 * i + j], fr, h0);
+          split_digits<S>(x[8 * i + j + 1], fr, h1);
+          // the bf16 halves of k = j (low) and j + 1 (high)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          uint32_t h[S];
-          split_digits<S>(x[8 * i + j], fr, h);
-#pragma unroll
-          for (int p = 0; p < S; ++p) w[p][j >> 1] |= h[p] << (16 * (j & 1));
+          for (int p = 0; p < S; ++p) w[p][j >> 1] = __byte_perm(h0[p], h1[p], 0x7632u);
         }
         uint8_t* c = img + stage_chunk<ROWS>(r, g);
 #pragma unroll
