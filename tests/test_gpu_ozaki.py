@@ -191,6 +191,28 @@ def test_ozaki_row_chunking_identical(ta, world, monkeypatch):
     assert np.array_equal(got.download(), ref.download())
 
 
+@pytest.mark.parametrize("n,kind", [(1100, 0), (6000, 1)])
+def test_ozaki_epilogue_widths_identical(ta, world, monkeypatch, n, kind):
+    """The eight-warp and sixteen-warp epilogues (chosen by the units'
+    average stage count, forced here) fold the same levels into the same
+    integers: results are bit-identical, on short and long k."""
+    hk = uneven(n, 48, 256, 23)
+    hm = uneven(700, 48, 256, 24)
+    A, _ = gpu_operand(ta, world, [hm, hk], 5, 0, kind=kind)
+    B, _ = gpu_operand(ta, world, [hk, hm], 5, 1, kind=kind)
+    alpha = 0.75 if kind == 0 else 1.0
+    out = {}
+    for w in ("8", "16"):
+        monkeypatch.setenv("TAGPU_EPILOGUE_WARPS", w)
+        C, _ = ta.contract(world, "i,j", alpha, A, "i,k", B, "k,j",
+                           precision=ta.PRECISION_OZAKI)
+        out[w] = C.download()
+    assert np.array_equal(out["8"], out["16"])
+    if kind == 1:   # integer data: exact, equal to the plain form
+        Cp, _ = ta.contract(world, "i,j", alpha, A, "i,k", B, "k,j")
+        assert np.array_equal(out["8"], Cp.download())
+
+
 def test_ozaki_autotune_identical_and_cached(ta, world, tmp_path, monkeypatch):
     """The autotuner only changes the schedule: results are bit-identical; the
     chosen schedule is cached per shape bucket."""

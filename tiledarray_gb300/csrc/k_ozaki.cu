@@ -92,8 +92,27 @@ __device__ __forceinline__ uint32_t drain_mask(int64_t x, int64_t n) {
 }
 constexpr int A_SLICE_BYTES = BM * BK * 2;   // 8 KB
 constexpr int B_SLICE_BYTES = BN * BK * 2;   // 4 KB
-constexpr int EPI_WARPS = 8;
-constexpr int THREADS = 64 + EPI_WARPS * 32; // producer, MMA, 8 epilogue warps
+// Epilogue warps: EW of them, four per 32-lane quarter of tensor memory,
+// each owning kCols of the block's 64 columns, and results staged kPass
+// columns at a time (row stride kPass + 1 doubles: the row-per-lane writes
+// hit distinct bank pairs per half warp).  Eight warps of 32 columns keep
+// 168 registers a thread for the MMA issue of long-k blocks; sixteen warps
+// of 16 columns (96 registers: five warps share a scheduler's register file)
+// hold half the accumulators per thread and hide twice the conversion
+// latency, which pays where blocks are short and the epilogue bounds the
+// kernel.
+template <int EW>
+struct Epi {
+  static_assert(EW == 8 || EW == 16, "eight or sixteen epilogue warps");
+  static constexpr int kCols = BN * 4 / EW;            // 32 or 16
+  static constexpr int kThreads = 64 + EW * 32;        // producer, MMA, epilogue warps
+  static constexpr int kPass = EW == 8 ? 16 : 8;
+  static constexpr int kLd = kPass + 1;
+  static constexpr int kBytes = EW * 32 * kLd * 8;     // 34,816 or 36,864
+};
+// Launches whose units average at most this many 32-k stages take sixteen
+// epilogue warps.
+constexpr int64_t kShortStages = 128;
 // Bound of the waits that let in-flight copies and MMAs finish before a CTA
 // exits (they end within microseconds; the bound only keeps a broken launch
 // from spinning forever).  The pipeline waits take their bound from the
@@ -315,16 +334,11 @@ struct OzParams {
   int* err;                  // error flag (0 = ok)
 };
 
-// Epilogue staging: per epilogue warp, 32 rows x 16 columns of results
-// (row stride 17 doubles: the row-per-lane writes and the column-per-lane
-// reads both hit 32 distinct banks pairs).
-constexpr int EPI_LD = 17;
-constexpr int EPI_BYTES = EPI_WARPS * 32 * EPI_LD * 8;   // 34,816
-template <int S>
+template <int S, int EW>
 struct Smem {
   static constexpr int kStages = (S * (A_SLICE_BYTES + B_SLICE_BYTES) * 3 <= 200 * 1024) ? 3 : 2;
   static constexpr int kStageBytes = S * (A_SLICE_BYTES + B_SLICE_BYTES);
-  static constexpr int kBytes = kStages * kStageBytes + EPI_BYTES + 1024;
+  static constexpr int kBytes = kStages * kStageBytes + Epi<EW>::kBytes + 1024;
 };
 
 // ---------------------------------------------------------------------------
@@ -580,13 +594,17 @@ __device__ __forceinline__ void stage_dispatch(int s, int e, uint32_t tmem, uint
 // Lazy zeroing: a level restarts by being marked fresh; the first MMA that
 // writes a fresh level does so with accumulate off.  A level still fresh at a
 // drain got no product in its period, and the epilogue skips it.
-template <int S, bool Q>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_gemm_kernel(
+template <int S, bool Q, int EW>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(Epi<EW>::kThreads, 1) ozaki_gemm_kernel(
     const OzParams* __restrict__ views, const int64_t* __restrict__ vstart, int nviews,
     int64_t nblk_total, int* __restrict__ err, unsigned long long wait_ns,
     const QueueArgs* __restrict__ qa) {
-  constexpr int STAGES = Smem<S>::kStages;
-  constexpr int STAGE_BYTES = Smem<S>::kStageBytes;
+  constexpr int STAGES = Smem<S, EW>::kStages;
+  constexpr int STAGE_BYTES = Smem<S, EW>::kStageBytes;
+  constexpr int EPI_WARPS = EW;
+  constexpr int EPI_COLS = Epi<EW>::kCols;
+  constexpr int EPI_PASS = Epi<EW>::kPass;
+  constexpr int EPI_LD = Epi<EW>::kLd;
   // levels 2..TOP are MMA targets: S + 1 of them and up to two extra, as
   // many as the 512 tensor-memory columns hold (one extra for S = 7)
   constexpr int TOP = S + 3 < 9 ? S + 3 : 9;
@@ -620,9 +638,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
     mbar_init(smem_u32(&bar_done), 1);
     for (int i = 0; i < 4; ++i) {
       mbar_init(smem_u32(&q_full[i]), 1);
-      // consumers of a slot: MMA + 8 epilogue warps of rank 0, producer, MMA
-      // and 8 epilogue warps of rank 1 (only rank 0's barrier is used)
-      mbar_init(smem_u32(&q_empty[i]), 19);
+      // consumers of a slot: MMA + epilogue warps of rank 0, producer, MMA
+      // and epilogue warps of rank 1 (only rank 0's barrier is used)
+      mbar_init(smem_u32(&q_empty[i]), 3 + 2 * EPI_WARPS);
     }
     mbar_init(smem_u32(&epi_done), EPI_WARPS);
     abort_s = 0;
@@ -1016,8 +1034,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
     }
   } else {
     // ------------------------------------------------------------ epilogue
-    // Eight warps: warp % 4 selects the 32 tensor-memory lanes (rows) a warp
-    // may access, (warp - 2) / 4 the half of the 64 columns it owns.  After
+    // warp % 4 selects the 32 tensor-memory lanes (rows) a warp may access,
+    // (warp - 2) / 4 the EPI_COLS of the 64 columns it owns.  After
     // each stage that ends a level's period (drain_mask), that level is read
     // (unless it got no product in the period), released to the MMA warp at
     // once, and folded into two int64 accumulators per element: hi in units
@@ -1026,14 +1044,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
     // units of level TOP takes the whole-block levels (L_t * 2^(8(TOP-t)),
     // t >= 6, each read once per block, below 2^59 together).
     const int quarter = warp & 3;
-    const int half = (warp - 2) >> 2;
+    const int cq = (warp - 2) >> 2;
     const int rloc = quarter * 32 + lane;
-    const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16) + half * 32;
+    const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16) + cq * EPI_COLS;
     int64_t events = 0;
     bool ok = true;
-    int64_t hi[32], lo[32];
+    int64_t hi[EPI_COLS], lo[EPI_COLS];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) hi[j] = lo[j] = 0;
+    for (int j = 0; j < EPI_COLS; ++j) hi[j] = lo[j] = 0;
     int64_t gb = unit0;
     uint32_t nunits = 0;
     for (;;) {
@@ -1077,7 +1095,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
           }
           float v0[16], v1[16];
           tmem_ld16(lane_addr + (t - 2) * BN, v0);
-          tmem_ld16(lane_addr + (t - 2) * BN + 16, v1);
+          if constexpr (EPI_COLS == 32) tmem_ld16(lane_addr + (t - 2) * BN + 16, v1);
           tmem_wait_ld();
           tc_fence_before();
           __syncwarp();   // every lane's reads are done: one arrival per warp
@@ -1088,14 +1106,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
               lo[j] += (int64_t)__float2ll_rn(v0[j]) << sh;
-              lo[16 + j] += (int64_t)__float2ll_rn(v1[j]) << sh;
+              if constexpr (EPI_COLS == 32) lo[16 + j] += (int64_t)__float2ll_rn(v1[j]) << sh;
             }
           } else {
             const int sh = 8 * (kExactTop - t);
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
               hi[j] += (int64_t)__float2int_rn(v0[j]) << sh;
-              hi[16 + j] += (int64_t)__float2int_rn(v1[j]) << sh;
+              if constexpr (EPI_COLS == 32) hi[16 + j] += (int64_t)__float2int_rn(v1[j]) << sh;
             }
           }
         }
@@ -1103,14 +1121,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
       if (!ok) break;
       // recombination: C = alpha * 2^(E_A + E_B - 8 M) * (hi * 2^(8(TOP-5)) + lo) * u_TOP,
       // exact integer to correctly rounded double, then one multiply by alpha.
-      // The column data of the warp's 32 columns is loaded one column per
-      // lane and broadcast by shuffles, the row's per thread, and the tile
-      // offset once per result tile crossed: every load is issued before the
-      // first store, so the stores do not serialise reloads behind them.
+      // The column data of the warp's EPI_COLS columns is loaded one column
+      // per lane and broadcast by shuffles, the row's per thread, and the
+      // tile offset once per result tile crossed: every load is issued before
+      // the first store, so the stores do not serialise reloads behind them.
       {
         const uint32_t full = 0xffffffffu;
-        const int64_t gcl = (int64_t)cb * BN + half * 32 + lane;
-        const bool cok = gcl < P.N_total;
+        const int64_t gcl = (int64_t)cb * BN + cq * EPI_COLS + lane;
+        const bool cok = lane < EPI_COLS && gcl < P.N_total;
         const int tj_l = cok ? P.col_tile[gcl] : -1;
         const int cl_l = cok ? P.col_local[gcl] : 0;
         const int eb_l = cok ? P.EB[gcl] - 1022 : 0;
@@ -1128,29 +1146,30 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
         const bool unit_alpha = alpha == 1.0;
         double* sb = reinterpret_cast<double*>(stage_base + STAGES * STAGE_BYTES) +
                      (warp - 2) * 32 * EPI_LD;
-        // Two passes of 16 columns: each lane converts its row's values into
-        // the warp's staging rows, then the warp writes them out with lane
-        // = column (lanes 0-15 one row, 16-31 the next), so every store
-        // instruction writes two 128-byte row segments.
+        // Passes of EPI_PASS columns: each lane converts its row's values
+        // into the warp's staging rows, then the warp writes them out with
+        // lane = column (32 / EPI_PASS rows at a time), so every store
+        // instruction writes whole 8 * EPI_PASS-byte row segments.
 #pragma unroll
-        for (int hc = 0; hc < 2; ++hc) {
+        for (int hc = 0; hc < EPI_COLS / EPI_PASS; ++hc) {
 #pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            const int j = 16 * hc + c;
+          for (int c = 0; c < EPI_PASS; ++c) {
+            const int j = EPI_PASS * hc + c;
             const int eb = __shfl_sync(full, eb_l, j);
             const double v = exact_to_double<8 * (TOP - kExactTop)>(hi[j], lo[j], e2 + eb);
             sb[lane * EPI_LD + c] = unit_alpha ? v : alpha * v;
           }
           __syncwarp();
-          const int c = lane & 15;
-          const int tj = __shfl_sync(full, tj_l, 16 * hc + c);
-          const int cl = __shfl_sync(full, cl_l, 16 * hc + c);
-          const int64_t nn = __shfl_sync(full, nn_l, 16 * hc + c);
+          const int c = lane % EPI_PASS;
+          const int tj = __shfl_sync(full, tj_l, EPI_PASS * hc + c);
+          const int cl = __shfl_sync(full, cl_l, EPI_PASS * hc + c);
+          const int64_t nn = __shfl_sync(full, nn_l, EPI_PASS * hc + c);
           int ti_prev = -1;
           int64_t off = -1;
+          constexpr int RPS = 32 / EPI_PASS;   // rows per store instruction
 #pragma unroll 4
-          for (int i = 0; i < 16; ++i) {
-            const int r = 2 * i + (lane >> 4);
+          for (int i = 0; i < 32 / RPS; ++i) {
+            const int r = RPS * i + lane / EPI_PASS;
             const int ti = __shfl_sync(full, ti_l, r);
             const int64_t mrow = __shfl_sync(full, mrow_l, r);
             if (ti >= 0 && tj >= 0) {
@@ -1165,9 +1184,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1) ozaki_ge
         }
       }
 #pragma unroll
-      for (int j = 0; j < 32; ++j) hi[j] = lo[j] = 0;
-          if constexpr (Q) {
-        // Each finished unit is counted per job once all eight warps have
+      for (int j = 0; j < EPI_COLS; ++j) hi[j] = lo[j] = 0;
+      if constexpr (Q) {
+        // Each finished unit is counted per job once all epilogue warps have
         // stored their results; the count reaching both CTAs of every unit
         // marks the job done for the host.
         __syncwarp();
@@ -1941,25 +1960,25 @@ constexpr int kMaxDevices = 128;
 
 // Co-resident clusters of the GEMM kernel on the current device (the
 // shared-memory attribute is set on first use, per device).
-template <int S, bool Q>
+template <int S, bool Q, int EW>
 int gemm_clusters(int sm_count) {
-  const size_t smem = Smem<S>::kBytes;
+  const size_t smem = Smem<S, EW>::kBytes;
   static bool set[kMaxDevices] = {};
   static int clusters[kMaxDevices] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= kMaxDevices) dev = 0;
   if (!set[dev]) {
-    cudaFuncSetAttribute(ozaki_gemm_kernel<S, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(ozaki_gemm_kernel<S, Q, EW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     // A persistent grid larger than what fits at once would leave the extra
     // clusters to start after others finish their whole share.
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(2 * (sm_count / 2)), 1, 1);
-    cfg.blockDim = dim3(THREADS, 1, 1);
+    cfg.blockDim = dim3(Epi<EW>::kThreads, 1, 1);
     cfg.dynamicSmemBytes = smem;
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, ozaki_gemm_kernel<S, Q>, &cfg) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveClusters(&n, ozaki_gemm_kernel<S, Q, EW>, &cfg) != cudaSuccess ||
         n <= 0) {
       cudaGetLastError();
       n = sm_count / 2;
@@ -1968,26 +1987,43 @@ int gemm_clusters(int sm_count) {
     set[dev] = true;
     if (const char* e = getenv("TAGPU_VERBOSE"))
       if (atoi(e) > 0)
-        fprintf(stderr, "tagpu: emulated GEMM (S=%d%s) on device %d: %d co-resident clusters "
-                "of 2 (%d SMs)\n", S, Q ? ", served" : "", dev, n, sm_count);
+        fprintf(stderr, "tagpu: emulated GEMM (S=%d%s, %d epilogue warps) on device %d: %d "
+                "co-resident clusters of 2 (%d SMs)\n", S, Q ? ", served" : "", EW, dev, n,
+                sm_count);
   }
   return clusters[dev];
 }
 
-template <int S>
-void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int64_t nblk,
-                   int* err, int sm_count, unsigned long long wait_ns, cudaStream_t st) {
-  const int clusters = gemm_clusters<S, false>(sm_count);
+template <int S, int EW>
+void launch_gemm_ew(const OzParams* views, const int64_t* vstart, int nviews, int64_t nblk,
+                    int* err, int sm_count, unsigned long long wait_ns, cudaStream_t st) {
+  const int clusters = gemm_clusters<S, false, EW>(sm_count);
   // clusters of two CTAs, one unit (pair of output blocks) at a time each
   const int64_t grid = 2 * std::min<int64_t>(nblk, clusters);
   if (grid > 0) {
     // stage shifts from the digit bricks just split, then the GEMM
     shift_kernel<<<blocks_for(nblk * 32, 256), 256, 0, st>>>(views, vstart, nviews, nblk, S);
     count_launch();
-    ozaki_gemm_kernel<S, false><<<(unsigned)grid, THREADS, Smem<S>::kBytes, st>>>(
-        views, vstart, nviews, nblk, err, wait_ns, nullptr);
+    ozaki_gemm_kernel<S, false, EW><<<(unsigned)grid, Epi<EW>::kThreads, Smem<S, EW>::kBytes,
+                                      st>>>(views, vstart, nviews, nblk, err, wait_ns, nullptr);
     count_launch();
   }
+}
+
+template <int S>
+void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int64_t nblk,
+                   int64_t nstages, int* err, int sm_count, unsigned long long wait_ns,
+                   cudaStream_t st) {
+  // TAGPU_EPILOGUE_WARPS=8 or 16 overrides the choice (results are the same)
+  bool wide = nstages <= kShortStages * nblk;
+  if (const char* e = getenv("TAGPU_EPILOGUE_WARPS")) {
+    const int w = atoi(e);
+    if (w == 8 || w == 16) wide = w == 16;
+  }
+  if (wide)
+    launch_gemm_ew<S, 16>(views, vstart, nviews, nblk, err, sm_count, wait_ns, st);
+  else
+    launch_gemm_ew<S, 8>(views, vstart, nviews, nblk, err, sm_count, wait_ns, st);
 }
 
 // The persistent served GEMM: all co-resident clusters but `reserve`, which
@@ -1995,9 +2031,9 @@ void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int
 template <int S>
 void launch_served_t(const QueueArgs* qa, int* err, int sm_count, int reserve,
                      unsigned long long wait_ns, cudaStream_t st) {
-  const int clusters = std::max(1, gemm_clusters<S, true>(sm_count) - reserve);
-  ozaki_gemm_kernel<S, true><<<(unsigned)(2 * clusters), THREADS, Smem<S>::kBytes, st>>>(
-      nullptr, nullptr, 0, 0, err, wait_ns, qa);
+  const int clusters = std::max(1, gemm_clusters<S, true, 8>(sm_count) - reserve);
+  ozaki_gemm_kernel<S, true, 8><<<(unsigned)(2 * clusters), Epi<8>::kThreads, Smem<S, 8>::kBytes,
+                                  st>>>(nullptr, nullptr, 0, 0, err, wait_ns, qa);
   count_launch();
 }
 
@@ -2438,34 +2474,39 @@ void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s) {
 }
 
 void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int nviews,
-                              int64_t nblk, int slices, int* d_err, int sm_count,
-                              unsigned long long wait_ns, cudaStream_t s) {
+                              int64_t nblk, int64_t nstages, int slices, int* d_err,
+                              int sm_count, unsigned long long wait_ns, cudaStream_t s) {
   const OzParams* v = static_cast<const OzParams*>(d_params);
+  const int64_t k = nstages;
   switch (slices) {
-    case 2: launch_gemm_t<2>(v, d_vstart, nviews, nblk, d_err, sm_count, wait_ns, s); break;
-    case 3: launch_gemm_t<3>(v, d_vstart, nviews, nblk, d_err, sm_count, wait_ns, s); break;
-    case 4: launch_gemm_t<4>(v, d_vstart, nviews, nblk, d_err, sm_count, wait_ns, s); break;
-    case 5: launch_gemm_t<5>(v, d_vstart, nviews, nblk, d_err, sm_count, wait_ns, s); break;
-    case 7: launch_gemm_t<7>(v, d_vstart, nviews, nblk, d_err, sm_count, wait_ns, s); break;
-    default: launch_gemm_t<6>(v, d_vstart, nviews, nblk, d_err, sm_count, wait_ns, s); break;
+    case 2: launch_gemm_t<2>(v, d_vstart, nviews, nblk, k, d_err, sm_count, wait_ns, s); break;
+    case 3: launch_gemm_t<3>(v, d_vstart, nviews, nblk, k, d_err, sm_count, wait_ns, s); break;
+    case 4: launch_gemm_t<4>(v, d_vstart, nviews, nblk, k, d_err, sm_count, wait_ns, s); break;
+    case 5: launch_gemm_t<5>(v, d_vstart, nviews, nblk, k, d_err, sm_count, wait_ns, s); break;
+    case 7: launch_gemm_t<7>(v, d_vstart, nviews, nblk, k, d_err, sm_count, wait_ns, s); break;
+    default: launch_gemm_t<6>(v, d_vstart, nviews, nblk, k, d_err, sm_count, wait_ns, s); break;
   }
 }
 
 void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s) {
   if (pl->nchunk == 1) {
-    ozaki_enqueue_gemm_views(pl->d_params, pl->d_vstart, 1, pl->nblk, pl->S, pl->err, sm_count,
-                             pl->wait_ns, s);
+    ozaki_enqueue_gemm_views(pl->d_params, pl->d_vstart, 1, pl->nblk, pl->nkb, pl->S, pl->err,
+                             sm_count, pl->wait_ns, s);
     return;
   }
   for (int c = 0; c < pl->nchunk; ++c) {
     launch_split(pl->S, pl->d_split_a + c, 1, pl->h_split_a[c].nbricks, true, sm_count, s);
-    ozaki_enqueue_gemm_views(pl->d_chunk_params + c, pl->d_chunk_vstart + 2 * c, 1,
-                             pl->chunk_blk[c + 1] - pl->chunk_blk[c], pl->S, pl->err, sm_count,
-                             pl->wait_ns, s);
+    // a chunk's units take the plan's average stage count
+    const int64_t units = pl->chunk_blk[c + 1] - pl->chunk_blk[c];
+    const int64_t stages = pl->nblk ? (int64_t)((double)pl->nkb * units / pl->nblk) : 0;
+    ozaki_enqueue_gemm_views(pl->d_chunk_params + c, pl->d_chunk_vstart + 2 * c, 1, units,
+                             stages, pl->S, pl->err, sm_count, pl->wait_ns, s);
   }
 }
 
 int ozaki_chunks(const OzakiPlan* pl) { return pl->nchunk; }
+
+int64_t ozaki_stages(const OzakiPlan* pl) { return pl->nkb; }
 
 namespace {
 template <typename T>

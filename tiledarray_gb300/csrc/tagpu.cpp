@@ -2107,6 +2107,7 @@ struct LaunchBufs {
   DBuf derr;                    // DMMA error flag (a bounded stage wait ran out)
   DBuf ozp[8], ozv[8];          // emulated form: parameter blocks, block offsets
   int64_t oz_nblk[8] = {0};
+  int64_t oz_nkb[8] = {0};   // 32-k stages of the group's units
   // emulated form, per digit count: job tables of the grouped zeroing,
   // frame and split launches
   DBuf gz[8], gf[8], gsa[8], gsb[8];
@@ -2232,10 +2233,13 @@ tagpu_status enqueue_gemms(tagpu_ctx* ctx, std::vector<Contraction*>& cs, Launch
       if ((e = upload_vec(ctx, lb.ozp[S], params)) || (e = upload_vec(ctx, lb.ozv[S], vstart)))
         return e;
       lb.oz_nblk[S] = vstart.back();
+      lb.oz_nkb[S] = 0;
+      for (OzakiPlan* pl : g) lb.oz_nkb[S] += ozaki_stages(pl);
       if (stream != ctx->stream) CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     }
     ozaki_enqueue_gemm_views(lb.ozp[S].p, lb.ozv[S].as<int64_t>(), (int)g.size(), lb.oz_nblk[S],
-                             S, ozaki_error_flag(g[0]), ctx->sm_count, ctx->wait_ns, stream);
+                             lb.oz_nkb[S], S, ozaki_error_flag(g[0]), ctx->sm_count, ctx->wait_ns,
+                             stream);
   }
   if (!items.empty()) {
     if (!lb.derr.p) {
