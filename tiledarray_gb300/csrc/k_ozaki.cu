@@ -256,6 +256,20 @@ __host__ __device__ constexpr uint32_t idesc_n(int n) {
          ((uint32_t)(BM >> 4) << 24);
 }
 
+// f * 2^sh as an exact int64, for an integer-valued float f with
+// |f| * 2^sh < 2^62, from the float's bits (mantissa shifted by its
+// exponent; zero shifts by at least 118 places down, clamped to 31).  The
+// 16-warp epilogue uses it instead of a conversion instruction, which runs
+// on this GPU's narrow FP64 pipe with a long latency; the 8-warp epilogue,
+// short of issue slots rather than latency, keeps the instruction.
+__device__ __forceinline__ int64_t float_to_ll_exact(float f, int sh) {
+  const uint32_t b = __float_as_uint(f);
+  const int e = (int)((b >> 23) & 0xff) - 150 + sh;
+  const uint32_t m = (b & 0x7fffffu) | 0x800000u;
+  const int64_t v = e >= 0 ? (int64_t)((uint64_t)m << e) : (int64_t)(m >> min(-e, 31));
+  return (int)b < 0 ? -v : v;
+}
+
 // Correctly rounded double of (hi * 2^SH + lo) * 2^e2 from exact integers
 // (|hi| < 2^61, |lo| < 2^62, 0 <= SH <= 32).  The value is first cut to a
 // signed 64-bit window with the bits cut off ORed into its lowest bit
@@ -1105,8 +1119,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(Epi<EW>::kThreads, 1
             const int sh = 8 * (TOP - t);
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-              lo[j] += (int64_t)__float2ll_rn(v0[j]) << sh;
-              if constexpr (EPI_COLS == 32) lo[16 + j] += (int64_t)__float2ll_rn(v1[j]) << sh;
+              if constexpr (EPI_COLS == 32) {
+                lo[j] += (int64_t)__float2ll_rn(v0[j]) << sh;
+                lo[16 + j] += (int64_t)__float2ll_rn(v1[j]) << sh;
+              } else {
+                lo[j] += float_to_ll_exact(v0[j], sh);
+              }
             }
           } else {
             const int sh = 8 * (kExactTop - t);
