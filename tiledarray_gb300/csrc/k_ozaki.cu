@@ -1383,12 +1383,14 @@ __global__ void __launch_bounds__(256) frame_kernel(const FrameJob* __restrict__
     const int kq = threadIdx.x / kFrameRows, nq = blockDim.x / kFrameRows;
     int e = 0;
     if (r < r1)
+#pragma unroll 4   // several loads in flight per thread
       for (int k = kq; k < kk; k += nq) e = max(e, exp_field(base[(int64_t)k * m + r]));
     if (e > 0) atomicMax(&Er[r], e);
   } else {                         // element (r, k) at r * kk + k
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int r = r0 + warp; r < r1; r += blockDim.x >> 5) {
       int e = 0;
+#pragma unroll 4
       for (int k = lane; k < kk; k += 32) e = max(e, exp_field(base[(int64_t)r * kk + k]));
       for (int s = 16; s > 0; s >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, s));
       if (lane == 0 && e > 0) atomicMax(&Er[r], e);
