@@ -3,38 +3,40 @@
 //
 // What is computed: the same per-result-tile reduction as the plain DMMA
 // kernel, C(i,j) = alpha * sum_k A(i,k) B(k,j) over the tile-pair list, with
-// an error against FP64 of order 2^-48 relative per product.
+// an error against FP64 of order 2^-(8S-1) relative per product (S = 7 by
+// default: every result tile within about 2e-14 of the FP64 oracle).
 //
 // How:
 //  * frames: every fused row r of A gets E_A[r] with |A[r,:]| < 2^E_A[r], every
 //    fused column c of B gets E_B[c] (one pass over the operands, integer ops
 //    on the IEEE bit fields);
-//  * splitting (integer only): a = x * 2^-E rounded to 8S-1 fractional bits is
-//    cut into S balanced base-256 digits d_1..d_S, |d_p| <= 128, so that
-//    a = sum_p d_p 2^(1-8p).  Digits are exact in bf16.  They are written into
-//    "bricks" (128 rows x 32 k for A, 64 columns x 32 k for B, in global fused
-//    coordinates) laid out exactly as the K-major no-swizzle UMMA operand image
-//    in shared memory, so one bulk copy moves a brick into place;
-//  * products: every pair (p, q) with p + q <= S + 1 adds D_p * E_q into the
-//    tensor-memory accumulator of level t = p + q with tcgen05.mma.kind::f16
-//    (bf16 x bf16 -> fp32, M=128, K=16); the levels are adjacent column
-//    ranges and the B slices adjacent in shared memory, so the pairs of one
-//    p form a single MMA of N = 64 * (S + 1 - p) (two above 256).  Every
-//    product is an integer below 2^14.  Level t (t-1 products per k)
-//    restarts from zero every 32, 16, 8, 8 stages of 32 k (t = 2..5; a power
-//    of two <= 32/(t-1), so restarts coincide), so levels 2..5 stay
-//    at or below 2^24 where every fp32 sum of integers is exact; levels 6
-//    and 7 (weight 2^-32 and 2^-40 against level 2) sum over the whole
-//    output block in fp32, a rounding below 2^-41 of sum_k |a b|;
+//  * splitting (integer only): operands are cut into "bricks" (128 rows x 32 k
+//    of A, 64 columns x 32 k of B, in global fused coordinates).  A brick's
+//    deficit e is the smallest number of bits by which a nonzero element sits
+//    below its row (column) frame; with m = floor(e / 8) whole digits, every
+//    element a = x * 2^-(E-8m) rounded to 8S-1 fractional bits is cut into S
+//    balanced base-256 digits d_1..d_S, |d_p| <= 128 (exact in bf16), a =
+//    sum_p d_p 2^(1-8p), written as the K-major no-swizzle UMMA operand image
+//    so that one bulk copy moves a brick into shared memory;
+//  * products: slice pair (p, q) of a stage whose bricks have shifts mA, mB
+//    lands on level t = p + q + mA + mB - M (M the output block's base), with
+//    tcgen05.mma.kind::f16 (bf16 x bf16 -> fp32, M = 128, K = 16) into the
+//    tensor-memory columns of level t (levels 2..TOP adjacent, 64 columns
+//    each, TOP = min(S + 3, 9)); compile-time stage programs group the
+//    products of one A slice into MMAs of several levels' width.  Levels
+//    2..5 restart every 32, 16, 8, 8 stages and stay exact in fp32; levels
+//    6..TOP sum over the whole block (the level comment below says why);
 //  * draining: when a level's period ends the epilogue warps read it,
 //    release it to the MMA warp at once through a per-level mbarrier (the
 //    MMAs of the slices that do not touch it never wait), and fold it into
-//    two int64 accumulators per element, hi = L2*2^8 + L3 and
-//    lo = sum_{t>=4} L_t*2^(8(S+1-t));
-//  * recombination (the only FP64 arithmetic): at the end of an output block
-//    C = alpha * 2^(E_A + E_B) * (hi*2^-22 + lo*2^(2-8(S+1))), written into
-//    the result tiles the block overlaps, while the MMA warp already runs the
-//    next block.
+//    two int64 accumulators per element: hi (units of level 5) takes the
+//    exact levels L_t * 2^(8(5-t)), lo (units of level TOP) the whole-block
+//    levels L_t * 2^(8(TOP-t));
+//  * recombination: at the end of an output block
+//    C = alpha * 2^(E_A + E_B - 8M) * (hi * 2^(8(TOP-5)) + lo) * 2^(2-8 TOP),
+//    the exact integer rounded once to double (exact_to_double), written
+//    into the result tiles the block overlaps while the MMA warp already
+//    runs the next block.
 // Work is in global fused coordinates (output blocks 128 x 64, k blocks of
 // 32), so uneven tiles cost no padding except at block-sparsity boundaries;
 // a brick is stored only if some nonzero tile overlaps it, a k block is run
