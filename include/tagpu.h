@@ -225,7 +225,7 @@ typedef struct tagpu_contract_opts {
                                  55-bit digits; 6 is faster, 47-bit) */
   float threshold;            /* result screening threshold, <0 = default */
   int autotune;               /* emulated form: time the GEMM schedules (block
-                                 order, accumulation chunk) on first use of a
+                                 order, epilogue width) on first use of a
                                  shape bucket and cache the fastest in the file
                                  named by TAGPU_TUNE_CACHE (results do not
                                  depend on the schedule); also enabled by the

@@ -214,8 +214,9 @@ def test_ozaki_epilogue_widths_identical(ta, world, monkeypatch, n, kind):
 
 
 def test_ozaki_autotune_identical_and_cached(ta, world, tmp_path, monkeypatch):
-    """The autotuner only changes the schedule: results are bit-identical; the
-    chosen schedule is cached per shape bucket."""
+    """The autotuner only changes the schedule (block order and epilogue
+    width): results are bit-identical; the chosen schedule is cached per
+    shape bucket, and a cache line without the width still reads."""
     cache = tmp_path / "tune.txt"
     monkeypatch.setenv("TAGPU_TUNE_CACHE", str(cache))
     h = uneven(900, 48, 200, 31)
@@ -226,8 +227,17 @@ def test_ozaki_autotune_identical_and_cached(ta, world, tmp_path, monkeypatch):
                          autotune=True)
     assert np.array_equal(got.download(), ref.download())
     lines = cache.read_text().split("\n")
-    assert lines[0].startswith("S7_") and len(lines[0].split()) == 4
+    fields = lines[0].split()
+    assert lines[0].startswith("S7_") and len(fields) == 5 and fields[4] in ("8", "16")
     again, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI,
                            autotune=True)
     assert np.array_equal(again.download(), ref.download())
     assert len([x for x in cache.read_text().split("\n") if x]) == 1
+    # a cache written before the width was tuned: four fields
+    old = tmp_path / "tune_old.txt"
+    old.write_text(" ".join(fields[:4]) + "\n")
+    monkeypatch.setenv("TAGPU_TUNE_CACHE", str(old))
+    legacy, _ = ta.contract(world, "i,j", 1.0, A, "i,k", B, "k,j", precision=ta.PRECISION_OZAKI,
+                            autotune=True)
+    assert np.array_equal(legacy.download(), ref.download())
+    assert len([x for x in old.read_text().split("\n") if x]) == 1

@@ -161,11 +161,13 @@ void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s);
 // One launch over the output blocks of several plans with the same slice
 // count: d_params holds their parameter blocks (ozaki_params), d_vstart the
 // prefix sums of their block counts; nstages their units' 32-k stages in
-// total (it picks the epilogue width); d_err receives a wait timeout (each
+// total (it picks the epilogue width unless epi_warps, 8 or 16, fixes it);
+// d_err receives a wait timeout (each
 // pipeline wait gives up after wait_ns).  Runs the stage-shift pass first.
 void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int nviews,
                               int64_t nblk, int64_t nstages, int slices, int* d_err,
-                              int sm_count, unsigned long long wait_ns, cudaStream_t s);
+                              int sm_count, unsigned long long wait_ns, cudaStream_t s,
+                              int epi_warps = 0);
 // 32-k stages over all units of a plan.
 int64_t ozaki_stages(const OzakiPlan* pl);
 // Number of row chunks (1 unless the A digit bricks would not fit at once;

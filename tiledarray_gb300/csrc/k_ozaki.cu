@@ -1926,6 +1926,7 @@ struct OzakiPlan {
   std::vector<int64_t> chunk_rb{0, 0};     // row-block boundaries of the chunks
   // schedule (results do not depend on it): super-tile of the block order
   int tune_gr = 4, tune_gc = 19;
+  int epi_warps = 0;   // epilogue width chosen by the autotuner, 0: by stage count
   std::vector<int32_t> h_blk;              // blocks (rb, cb) in discovery order
   std::vector<int64_t> h_off;              // their k-list offsets
   size_t bytes = 0;
@@ -2034,10 +2035,12 @@ void launch_gemm_ew(const OzParams* views, const int64_t* vstart, int nviews, in
 
 template <int S>
 void launch_gemm_t(const OzParams* views, const int64_t* vstart, int nviews, int64_t nblk,
-                   int64_t nstages, int* err, int sm_count, unsigned long long wait_ns,
-                   cudaStream_t st) {
-  // TAGPU_EPILOGUE_WARPS=8 or 16 overrides the choice (results are the same)
-  bool wide = nstages <= kShortStages * nblk;
+                   int64_t nstages, int epi_warps, int* err, int sm_count,
+                   unsigned long long wait_ns, cudaStream_t st) {
+  // the width from the autotuner (epi_warps 8 or 16), else by the units'
+  // average stage count; TAGPU_EPILOGUE_WARPS=8 or 16 overrides both
+  // (results are the same)
+  bool wide = epi_warps ? epi_warps == 16 : nstages <= kShortStages * nblk;
   if (const char* e = getenv("TAGPU_EPILOGUE_WARPS")) {
     const int w = atoi(e);
     if (w == 8 || w == 16) wide = w == 16;
@@ -2497,23 +2500,25 @@ void ozaki_enqueue(OzakiPlan* pl, int sm_count, cudaStream_t s) {
 
 void ozaki_enqueue_gemm_views(const void* d_params, const int64_t* d_vstart, int nviews,
                               int64_t nblk, int64_t nstages, int slices, int* d_err,
-                              int sm_count, unsigned long long wait_ns, cudaStream_t s) {
+                              int sm_count, unsigned long long wait_ns, cudaStream_t s,
+                              int epi_warps) {
   const OzParams* v = static_cast<const OzParams*>(d_params);
   const int64_t k = nstages;
+  const int w = epi_warps;
   switch (slices) {
-    case 2: launch_gemm_t<2>(v, d_vstart, nviews, nblk, k, d_err, sm_count, wait_ns, s); break;
-    case 3: launch_gemm_t<3>(v, d_vstart, nviews, nblk, k, d_err, sm_count, wait_ns, s); break;
-    case 4: launch_gemm_t<4>(v, d_vstart, nviews, nblk, k, d_err, sm_count, wait_ns, s); break;
-    case 5: launch_gemm_t<5>(v, d_vstart, nviews, nblk, k, d_err, sm_count, wait_ns, s); break;
-    case 7: launch_gemm_t<7>(v, d_vstart, nviews, nblk, k, d_err, sm_count, wait_ns, s); break;
-    default: launch_gemm_t<6>(v, d_vstart, nviews, nblk, k, d_err, sm_count, wait_ns, s); break;
+    case 2: launch_gemm_t<2>(v, d_vstart, nviews, nblk, k, w, d_err, sm_count, wait_ns, s); break;
+    case 3: launch_gemm_t<3>(v, d_vstart, nviews, nblk, k, w, d_err, sm_count, wait_ns, s); break;
+    case 4: launch_gemm_t<4>(v, d_vstart, nviews, nblk, k, w, d_err, sm_count, wait_ns, s); break;
+    case 5: launch_gemm_t<5>(v, d_vstart, nviews, nblk, k, w, d_err, sm_count, wait_ns, s); break;
+    case 7: launch_gemm_t<7>(v, d_vstart, nviews, nblk, k, w, d_err, sm_count, wait_ns, s); break;
+    default: launch_gemm_t<6>(v, d_vstart, nviews, nblk, k, w, d_err, sm_count, wait_ns, s); break;
   }
 }
 
 void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s) {
   if (pl->nchunk == 1) {
     ozaki_enqueue_gemm_views(pl->d_params, pl->d_vstart, 1, pl->nblk, pl->nkb, pl->S, pl->err,
-                             sm_count, pl->wait_ns, s);
+                             sm_count, pl->wait_ns, s, pl->epi_warps);
     return;
   }
   for (int c = 0; c < pl->nchunk; ++c) {
@@ -2522,7 +2527,7 @@ void ozaki_enqueue_gemm(OzakiPlan* pl, int sm_count, cudaStream_t s) {
     const int64_t units = pl->chunk_blk[c + 1] - pl->chunk_blk[c];
     const int64_t stages = pl->nblk ? (int64_t)((double)pl->nkb * units / pl->nblk) : 0;
     ozaki_enqueue_gemm_views(pl->d_chunk_params + c, pl->d_chunk_vstart + 2 * c, 1, units,
-                             stages, pl->S, pl->err, sm_count, pl->wait_ns, s);
+                             stages, pl->S, pl->err, sm_count, pl->wait_ns, s, pl->epi_warps);
   }
 }
 
@@ -2614,11 +2619,15 @@ tagpu_status ozaki_autotune(OzakiPlan* pl, int sm_count, cudaStream_t s, const c
       char line[256];
       while (fgets(line, sizeof(line), f)) {
         char k[128], extra[8];
-        int gr, gc;
+        int gr, gc, ew = 0;
         double ms;
-        if (sscanf(line, "%127s %d %d %lf %7s", k, &gr, &gc, &ms, extra) == 4 && key == k) {
+        // "bucket rows cols ms epilogue-warps" (lines without the width
+        // leave it to the stage count)
+        const int n = sscanf(line, "%127s %d %d %lf %d %7s", k, &gr, &gc, &ms, &ew, extra);
+        if ((n == 4 || n == 5) && key == k) {
           fclose(f);
           if (log) *log = "cached " + key;
+          pl->epi_warps = n == 5 && (ew == 8 || ew == 16) ? ew : 0;
           return ozaki_schedule(pl, gr, gc, err);
         }
       }
@@ -2626,6 +2635,7 @@ tagpu_status ozaki_autotune(OzakiPlan* pl, int sm_count, cudaStream_t s, const c
     }
   }
   ozaki_enqueue(pl, sm_count, s);  // frames and bricks for the timing runs
+  pl->epi_warps = 0;               // the block orders are timed with the width by stage count
   const int shapes[][2] = {{4, 19}, {2, 38}, {8, 10}, {1, 76}, {19, 4}, {6, 13}, {3, 25}, {12, 6}};
   std::string all;
   cudaEvent_t e0, e1;
@@ -2655,20 +2665,53 @@ tagpu_status ozaki_autotune(OzakiPlan* pl, int sm_count, cudaStream_t s, const c
       bgc = sh[1];
     }
   }
+  if (st) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return st;
+  }
+  if ((st = ozaki_schedule(pl, bgr, bgc, err))) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return st;
+  }
+  // the epilogue width: the best order above ran with the width the stage
+  // count picks; time the other one on it and keep the faster
+  const int auto_w = pl->nkb <= kShortStages * pl->nblk ? 16 : 8;
+  int best_w = auto_w;
+  {
+    pl->epi_warps = auto_w == 16 ? 8 : 16;
+    float t = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {
+      cudaEventRecord(e0, s);
+      ozaki_enqueue_gemm(pl, sm_count, s);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      t = std::min(t, ms);
+    }
+    char one[64];
+    snprintf(one, sizeof(one), "; %d warps on %dx%d:%.3f", pl->epi_warps, bgr, bgc, t);
+    all += one;
+    if (t < best) {
+      best = t;
+      best_w = pl->epi_warps;
+    }
+    pl->epi_warps = best_w;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (st) return st;
-  if ((st = ozaki_schedule(pl, bgr, bgc, err))) return st;
   if (cache && *cache) {
     if (FILE* f = fopen(cache, "a")) {
-      fprintf(f, "%s %d %d %.4f\n", key.c_str(), bgr, bgc, best);
+      fprintf(f, "%s %d %d %.4f %d\n", key.c_str(), bgr, bgc, best, best_w);
       fclose(f);
     }
   }
   if (log) {
     char buf[256];
-    snprintf(buf, sizeof(buf), "tuned %s: super-tile %dx%d, %.3f ms (ms per shape:", key.c_str(),
-             bgr, bgc, best);
+    snprintf(buf, sizeof(buf), "tuned %s: super-tile %dx%d, %d epilogue warps, %.3f ms (ms per "
+             "shape:", key.c_str(), bgr, bgc, best_w, best);
     *log = std::string(buf) + all + ")";
   }
   if (const char* e = getenv("TAGPU_VERBOSE"))
