@@ -3,10 +3,13 @@ on, restated in Python: the balanced base-256 digit split (the 64-bit
 recurrence and the biased-byte form the split kernel uses give the same
 digits, and the digits rebuild the fixed-point value), and the level restart
 periods (every exact level stays within 2^24, restarting levels form one
-run of adjacent levels)."""
+run of adjacent levels), and the recombination's two integer conversions
+(round to odd into a 64-bit window, float to int64 from its bits)."""
+import math
 import random
 import struct
 
+import numpy as np
 import pytest
 
 
@@ -81,3 +84,76 @@ def test_restarting_levels_form_one_run(S):
         if z:
             assert z == list(range(z[0], top + 1)), (x, z)
             assert x % 8 == 0
+
+
+# --- the recombination's conversions -------------------------------------
+
+def window_to_double(hi, lo, SH, e2):
+    """The kernel's exact_to_double<SH>: W = hi * 2^SH + lo is cut to a signed
+    64-bit window with the bits cut off ORed into its lowest bit (round to
+    odd), the window rounded once to double, then scaled by 2^e2 (normal
+    results only here)."""
+    if SH == 0:
+        y, scale = hi + lo, e2
+    else:
+        H = hi + (lo >> SH)
+        r = lo & ((1 << SH) - 1)
+        s = 63 - (H ^ (H >> 63)).bit_length()           # redundant sign bits of H (64-bit)
+        if s >= SH:
+            y, scale = (H << SH) | r, e2
+        else:
+            d = SH - s
+            y = (H << s) | (r >> d) | (1 if r & ((1 << d) - 1) else 0)
+            scale = e2 + d
+    assert -(1 << 63) <= y < (1 << 63)
+    return math.ldexp(float(y), scale) if y else 0.0
+
+
+@pytest.mark.parametrize("SH", [0, 8, 16, 24, 32])
+def test_round_to_odd_window_rounds_correctly(SH):
+    """Rounding to odd at 55 bits or more, then to 53, equals one correct
+    rounding of the exact value (checked against exact rational arithmetic;
+    Python's int / int is correctly rounded)."""
+    rng = random.Random(SH)
+    for it in range(20000):
+        mode = it % 5
+        hi = rng.randint(-(1 << 57), 1 << 57) >> rng.randint(0, 57)
+        lo = rng.randint(-(1 << 59), 1 << 59) >> rng.randint(0, 59)
+        if mode == 1:                                    # cancellation
+            hi = rng.randint(-(1 << 26), 1 << 26)
+            lo = -(hi << SH) + rng.randint(-(1 << 30), 1 << 30)
+        if mode == 2:                                    # ties in the low bits
+            lo = (lo >> 12) << 12 | (1 << 11)
+        if SH == 0:
+            hi = 0 if mode == 3 else hi
+        e2 = rng.randint(-900, 800)
+        W = (hi << SH) + lo
+        got = window_to_double(hi, lo, SH, e2)
+        if W == 0:
+            assert got == 0.0
+            continue
+        exact = float(W << e2) if e2 >= 0 else W / (1 << -e2)   # both correctly rounded
+        assert got == exact, (hi, lo, e2)
+
+
+def float_to_int64_from_bits(f32_bits, sh):
+    """The 16-warp epilogue's float_to_ll_exact: f * 2^sh for an
+    integer-valued float from its bits (mantissa shifted by its exponent)."""
+    e = ((f32_bits >> 23) & 0xFF) - 150 + sh
+    m = (f32_bits & 0x7FFFFF) | 0x800000
+    v = m << e if e >= 0 else m >> min(-e, 31)
+    return -v if f32_bits >> 31 else v
+
+
+@pytest.mark.parametrize("sh", [0, 8, 16, 24, 32])
+def test_float_to_int64_from_bits(sh):
+    rng = np.random.default_rng(sh)
+    # integer-valued floats across every exponent with |f| * 2^sh < 2^62
+    mags = np.concatenate([rng.integers(1, 1 << 24, 4000).astype(np.float64),
+                           np.ldexp(rng.integers(1 << 23, 1 << 24, 4000).astype(np.float64),
+                                    rng.integers(0, 62 - 24 - sh + 1, 4000))])
+    vals = np.concatenate([mags, -mags, [0.0, -0.0, 1.0, -1.0, 2.0 ** 24, -(2.0 ** 24)]])
+    f32 = vals.astype(np.float32)
+    assert np.array_equal(f32.astype(np.float64), vals)       # exactly representable
+    for v, b in zip(vals, f32.view(np.uint32)):
+        assert float_to_int64_from_bits(int(b), sh) == int(v) << sh, (v, sh)
